@@ -1,0 +1,143 @@
+// ctd_arith.cuh -- device modular arithmetic for the residue kernels.
+//
+// The reference reduces with Barrett multipliers mu64/mu128 recomputed per
+// prime (src/modular_arithmetic_detail.hpp:249-355, a 128/64 division per
+// prime).  Here the per-prime set-up (the jump to the first index of a tile)
+// uses Montgomery multiplication with R = 2^64 (Montgomery 1985), whose only
+// division-like step is a Newton iteration for p^-1 mod 2^64, and the
+// per-step loops use forms that need no division at all (doubling, addition,
+// and Shoup's precomputed-quotient multiplication for Smarandache).  Every
+// function returns the exact residue, so results equal the reference's.
+#pragma once
+
+#include <cstdint>
+
+#define CTD_HD __host__ __device__ __forceinline__
+
+namespace ctd {
+
+// ---------------------------------------------------------------- helpers
+CTD_HD uint64_t mulhi64(uint64_t a, uint64_t b)
+{
+#ifdef __CUDA_ARCH__
+    return __umul64hi(a, b);
+#else
+    return (uint64_t)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+CTD_HD uint32_t mulhi32(uint32_t a, uint32_t b)
+{
+#ifdef __CUDA_ARCH__
+    return __umulhi(a, b);
+#else
+    return (uint32_t)(((uint64_t)a * b) >> 32);
+#endif
+}
+
+// a + b mod p for a, b < p < 2^64 (no overflow assumptions)
+CTD_HD uint64_t addmod(uint64_t a, uint64_t b, uint64_t p)
+{
+    return a < p - b ? a + b : a - (p - b);
+}
+
+// a - b mod p for a, b < p
+CTD_HD uint64_t submod(uint64_t a, uint64_t b, uint64_t p)
+{
+    return a >= b ? a - b : p - (b - a);
+}
+
+// 2a mod p for a < p
+CTD_HD uint64_t dblmod(uint64_t a, uint64_t p)
+{
+    return a < p - a ? a << 1 : a - (p - a);
+}
+
+// ------------------------------------------------------- Montgomery, R=2^64
+// Values are kept in Montgomery form xR mod p, in [0, p).  Valid for every
+// odd p < 2^64: the REDC sum below keeps its carry.
+struct Mont {
+    uint64_t p;     // odd modulus
+    uint64_t pinv;  // -p^-1 mod 2^64
+    uint64_t one;   // R mod p
+    uint64_t r2;    // R^2 mod p
+
+    CTD_HD static uint64_t neg_inverse(uint64_t p)
+    {
+        // Newton-Hensel lifting: x <- x(2 - px) doubles the correct low bits;
+        // x = p is correct to 3 bits for odd p (p*p = 1 mod 8).
+        uint64_t x = p;
+        #pragma unroll
+        for (int i = 0; i < 5; ++i)
+            x *= 2 - p * x;
+        return (uint64_t)0 - x;
+    }
+
+    CTD_HD void init(uint64_t modulus)
+    {
+        p = modulus;
+        pinv = neg_inverse(p);
+        one = ((uint64_t)0 - p) % p;  // 2^64 mod p
+        // R^2 mod p = (R mod p) * 2^64 mod p by 64 modular doublings
+        uint64_t x = one;
+        #pragma unroll 8
+        for (int i = 0; i < 64; ++i)
+            x = dblmod(x, p);
+        r2 = x;
+    }
+
+    // a * b * R^-1 mod p for a, b < p
+    CTD_HD uint64_t mul(uint64_t a, uint64_t b) const
+    {
+        uint64_t lo = a * b;
+        uint64_t hi = mulhi64(a, b);
+        uint64_t m = lo * pinv;
+        uint64_t mh = mulhi64(m, p);
+        // (hi:lo + mh:ml) / 2^64, where lo + ml == 0 mod 2^64 with a carry iff lo != 0
+        uint64_t u = hi + mh;
+        bool ov = u < hi;
+        uint64_t c = lo != 0;
+        u += c;
+        ov |= u < c;
+        if (ov || u >= p)
+            u -= p;
+        return u;
+    }
+
+    CTD_HD uint64_t to(uint64_t x) const { return mul(x % p, r2); }
+    CTD_HD uint64_t from(uint64_t X) const { return mul(X, 1); }
+    CTD_HD uint64_t add(uint64_t a, uint64_t b) const { return addmod(a, b, p); }
+    CTD_HD uint64_t sub(uint64_t a, uint64_t b) const { return submod(a, b, p); }
+    CTD_HD uint64_t dbl(uint64_t a) const { return dblmod(a, p); }
+
+    // (2^e) in Montgomery form, left-to-right binary powering by doubling
+    CTD_HD uint64_t pow2(uint64_t e) const
+    {
+        uint64_t two = dbl(one);
+        return pow(two, e);
+    }
+
+    // base^e in Montgomery form (base in Montgomery form)
+    CTD_HD uint64_t pow(uint64_t base, uint64_t e) const
+    {
+        uint64_t r = one;
+        while (e) {
+            if (e & 1)
+                r = mul(r, base);
+            base = mul(base, base);
+            e >>= 1;
+        }
+        return r;
+    }
+};
+
+// ------------------------------------------------------ Shoup, 32-bit words
+// x * w mod p with the precomputed quotient ws = floor(w * 2^32 / p)
+// (Shoup, "NTL: A library for doing number theory"; also Harvey 2014).
+// For any x < 2^32 and w < p < 2^31 the result lies in [0, 2p).
+CTD_HD uint32_t shoup_precompute32(uint32_t w, uint32_t p)
+{
+    return (uint32_t)(((uint64_t)w << 32) / p);
+}
+
+}  // namespace ctd

@@ -1,0 +1,81 @@
+// ctd_internal.h -- internal C++ interface between the C-ABI layer
+// (ctd_engine.cu), the device sieve (ctd_sieve.cu) and the residue kernels
+// (ctd_residue.cu).  Not installed; the public boundary is include/ctd_gpu.h.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "../../include/ctd_gpu.h"
+
+namespace ctd {
+
+// Family ids: the numbering of the reference's num_seq_id
+// (src/num_seq_id.hpp:16-26); PEANO is its test-only S(n) = n sequence
+// (tests/peano.hpp:127-137).
+enum Family : uint32_t {
+    MERSENNE = CTD_MERSENNE,
+    PROTH = CTD_PROTH,
+    RIESEL = CTD_RIESEL,
+    SMARANDACHE = CTD_SMARANDACHE,
+    FIBONACCI = CTD_FIBONACCI,
+    LUCAS = CTD_LUCAS,
+    PROTH_FIXED_N = CTD_PROTH_FIXED_N,
+    RIESEL_FIXED_N = CTD_RIESEL_FIXED_N,
+    TRIBONACCI = CTD_TRIBONACCI,
+    PEANO = CTD_PEANO,
+};
+
+// Device view of one job's factors buffer, in the reference layout
+// (src/factors_buffer.hpp:77-86): counts[N], factors[N * max_factors],
+// slot order = arrival order.
+struct FactorsView {
+    uint32_t *counts;
+    uint64_t *factors;
+    uint32_t max_factors;
+};
+
+// What a residue launch needs to know about its job.
+struct JobView {
+    uint32_t family;
+    uint32_t tiles;      // index tiles per prime (>= 1)
+    uint64_t param;      // k, n or base
+    uint64_t n0, n1;     // index range of the factors buffer
+    uint64_t tile_len;   // indices per tile (last tile may be shorter)
+    FactorsView fb;
+};
+
+// Status word written by kernels that can fail on the device (bounded
+// waits, capacity checks); 0 = ok.
+struct DeviceStatus {
+    uint32_t code;
+    uint32_t detail;
+};
+
+// ---------------------------------------------------------------- sieve
+// Primes in [lo, hi) (ascending) written to d_out; *count receives the
+// number of primes (the list is truncated at `capacity`).  Scratch is the
+// sieve's own (SieveWorkspace); all work is queued on `stream`, which is
+// synchronized once to read the count.
+struct SieveWorkspace;
+SieveWorkspace *sieve_workspace_create();
+void sieve_workspace_destroy(SieveWorkspace *ws);
+int sieve_range(SieveWorkspace *ws, uint64_t lo, uint64_t hi, uint64_t *d_out, uint64_t capacity,
+                uint64_t *count, cudaStream_t stream, std::string &err);
+// Upper bound on the number of primes in [lo, hi) (for buffer sizing).
+uint64_t prime_count_upper_bound(uint64_t lo, uint64_t hi);
+
+// -------------------------------------------------------------- residues
+// Odd primes only.  Launches the family's residue kernel over
+// nprimes x view.tiles work items.
+int launch_residues(const JobView &view, const uint64_t *d_primes, uint64_t nprimes, int grid, int block,
+                    cudaStream_t stream, std::string &err);
+// The prime 2: the reference's serial mod-2 pass (src/trial_factoring.cuh:139-154).
+int launch_mod2(const JobView &view, cudaStream_t stream, std::string &err);
+// Number of kernel launches issued by this process so far (diagnostics).
+uint64_t kernel_launch_count();
+void note_kernel_launch();
+
+}  // namespace ctd

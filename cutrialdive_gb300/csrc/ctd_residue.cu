@@ -1,0 +1,579 @@
+// ctd_residue.cu -- residue-propagation kernels for every sequence family.
+//
+// One work item = (odd prime p, index tile [s, e)).  The item jumps to
+// S(s) mod p with a per-family O(log s) method, then walks the recurrence
+// e-s-1 steps, pushing p into the factors buffer of every index whose
+// residue is zero.  This is the work of trial_div_by_odd_primes
+// (src/trial_factoring.cuh:156-228) and of its CPU twin
+// trial_factorer::process_chunk (src/trial_factoring_impl.hpp:193-248),
+// re-planned for the GPU:
+//   * each family walks an equivalent recurrence with the fewest integer
+//     operations per step (doubling / addition / Shoup multiply) and a
+//     32-bit candidate test, replaying the few candidate blocks exactly;
+//   * the jump makes any index tile a unit of work, so short prime lists
+//     still fill the GPU (the reference walks [n0, n1) per prime only).
+// Hits are exact: a prime is pushed for index n iff p | S(n), exactly the
+// set the reference's Barrett propagation yields.
+#include "ctd_arith.cuh"
+#include "ctd_internal.h"
+
+#include <atomic>
+
+namespace ctd {
+
+namespace {
+std::atomic<uint64_t> g_launches{0};
+}
+
+void note_kernel_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+uint64_t kernel_launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
+// ----------------------------------------------------------------- push
+// factors_buffer push (src/device_factors_buffer.hpp:119-129): atomic slot
+// reservation, store only below the per-term capacity; the count keeps
+// growing so overflow is visible to the host.
+__device__ __forceinline__ void push(const FactorsView &fb, uint64_t idx, uint64_t p)
+{
+    uint32_t pos = atomicAdd(&fb.counts[idx], 1u);
+    if (pos < fb.max_factors)
+        fb.factors[idx * fb.max_factors + pos] = p;
+}
+
+// ------------------------------------------------------- step primitives
+// 2u mod p and u + c mod p for p < 2^63: one wrapped subtraction and a sign
+// test instead of a compare-and-select on the unreduced value.
+__device__ __forceinline__ uint64_t dbl63(uint64_t u, uint64_t p)
+{
+    uint64_t v = (u << 1) - p;
+    return ((int64_t)v < 0) ? v + p : v;
+}
+
+__device__ __forceinline__ uint64_t add63(uint64_t u, uint64_t c, uint64_t p)
+{
+    uint64_t v = u + c - p;
+    return ((int64_t)v < 0) ? v + p : v;
+}
+
+constexpr int UNROLL = 8;
+
+// Walks u -> step(u) for `steps` steps from index `idx`, pushing p wherever
+// u == target.  The unrolled body only tests the low 32 bits (one compare
+// per step); a block whose low words matched is replayed with the full test.
+template <class Step>
+__device__ __forceinline__ void walk_target(uint64_t u, uint64_t target, uint64_t p, uint64_t idx, uint64_t steps,
+                                            const FactorsView &fb, Step step)
+{
+    if (u == target)
+        push(fb, idx, p);
+    const uint32_t tlo = (uint32_t)target;
+    uint64_t i = 0;
+    for (; i + UNROLL <= steps; i += UNROLL) {
+        const uint64_t u0 = u;
+        bool cand = false;
+#pragma unroll
+        for (int j = 0; j < UNROLL; ++j) {
+            u = step(u);
+            cand |= ((uint32_t)u == tlo);
+        }
+        if (cand) {
+            uint64_t v = u0;
+#pragma unroll 1
+            for (int j = 0; j < UNROLL; ++j) {
+                v = step(v);
+                if (v == target)
+                    push(fb, idx + i + j + 1, p);
+            }
+        }
+    }
+    for (; i < steps; ++i) {
+        u = step(u);
+        if (u == target)
+            push(fb, idx + i + 1, p);
+    }
+}
+
+// ------------------------------------------------------------- families
+
+// Proth k*2^n+1, Riesel k*2^n-1, Mersenne 2^n-1 (riesel_proth.hpp:90-115,
+// mersenne.hpp:256-303).  With u(n) = k*2^n mod p the recurrence
+// S(n+1) = 2S(n) -+ 1 becomes pure doubling, and S(n) = 0 mod p becomes
+// u == p-1 (Proth) or u == 1 (Riesel, Mersenne).
+template <uint32_t FAM>
+__device__ __forceinline__ void run_doubling(const JobView &job, uint64_t p, uint64_t s, uint64_t e)
+{
+    Mont m;
+    m.init(p);
+    uint64_t U = m.pow2(s);
+    if (FAM != MERSENNE)
+        U = m.mul(U, m.to(job.param));
+    const uint64_t u = m.from(U);
+    const uint64_t target = (FAM == PROTH) ? p - 1 : 1;
+    const uint64_t steps = e - s - 1;
+    if (p < (1ull << 63))
+        walk_target(u, target, p, s - job.n0, steps, job.fb, [p](uint64_t x) { return dbl63(x, p); });
+    else
+        walk_target(u, target, p, s - job.n0, steps, job.fb, [p](uint64_t x) { return dblmod(x, p); });
+}
+
+// k*2^n +- 1 with fixed n over the index k (riesel_proth_fixed_n.hpp:88-151):
+// v(k) = k*2^n mod p grows by c = 2^n mod p per index; S(k) = 0 iff
+// v == p-1 (Proth) or v == 1 (Riesel).
+template <uint32_t FAM>
+__device__ __forceinline__ void run_fixed_n(const JobView &job, uint64_t p, uint64_t s, uint64_t e)
+{
+    Mont m;
+    m.init(p);
+    const uint64_t C = m.pow2(job.param);
+    const uint64_t c = m.from(C);
+    const uint64_t v = m.from(m.mul(m.to(s), C));
+    const uint64_t target = (FAM == PROTH_FIXED_N) ? p - 1 : 1;
+    const uint64_t steps = e - s - 1;
+    if (p < (1ull << 63))
+        walk_target(v, target, p, s - job.n0, steps, job.fb, [p, c](uint64_t x) { return add63(x, c, p); });
+    else
+        walk_target(v, target, p, s - job.n0, steps, job.fb, [p, c](uint64_t x) { return addmod(x, c, p); });
+}
+
+// (F(k), F(k+1)) mod p in Montgomery form by the doubling identities
+// F(2j) = F(j)(2F(j+1) - F(j)), F(2j+1) = F(j)^2 + F(j+1)^2.
+__device__ __forceinline__ void fib_pair(const Mont &m, uint64_t k, uint64_t &fk, uint64_t &fk1)
+{
+    uint64_t a = 0, b = m.one;
+    for (int bit = 63 - (k ? __clzll(k) : 63); k && bit >= 0; --bit) {
+        uint64_t c = m.mul(a, m.sub(m.dbl(b), a));
+        uint64_t d = m.add(m.mul(a, a), m.mul(b, b));
+        if ((k >> bit) & 1) {
+            a = d;
+            b = m.add(c, d);
+        } else {
+            a = c;
+            b = d;
+        }
+    }
+    fk = a;
+    fk1 = b;
+}
+
+// Fibonacci / Lucas: state (S(n-1), S(n)), one addmod per step
+// (fibonacci.hpp:245-285, lucas.hpp:394-418).  The reference's
+// make_state(0) leaves S(-1) = 0 and S(0) = 0, so a job starting at n0 = 0
+// propagates zeros: every prime is recorded for every term.  That behaviour
+// is kept (it is what the reference outputs).
+template <uint32_t FAM>
+__device__ __forceinline__ void run_fibonacci(const JobView &job, uint64_t p, uint64_t s, uint64_t e)
+{
+    uint64_t a = 0, b = 0;  // (S(s-1), S(s))
+    if (job.n0 != 0 && s != 0) {
+        Mont m;
+        m.init(p);
+        uint64_t F0, F1;  // F(s-1), F(s)
+        fib_pair(m, s - 1, F0, F1);
+        if (FAM == LUCAS) {
+            // L(s-1) = 2F(s) - F(s-1), L(s) = F(s) + 2F(s-1)
+            uint64_t L0 = m.sub(m.dbl(F1), F0);
+            uint64_t L1 = m.add(F1, m.dbl(F0));
+            F0 = L0;
+            F1 = L1;
+        }
+        a = m.from(F0);
+        b = m.from(F1);
+    }
+    uint64_t idx = s - job.n0;
+    const uint64_t steps = e - s - 1;
+    if (b == 0)
+        push(job.fb, idx, p);
+    uint64_t i = 0;
+    if (p < (1ull << 63)) {
+        for (; i + UNROLL <= steps; i += UNROLL) {
+            const uint64_t a0 = a, b0 = b;
+            bool cand = false;
+#pragma unroll
+            for (int j = 0; j < UNROLL; ++j) {
+                uint64_t c = add63(a, b, p);
+                a = b;
+                b = c;
+                cand |= ((uint32_t)c == 0u);
+            }
+            if (cand) {
+                uint64_t x = a0, y = b0;
+#pragma unroll 1
+                for (int j = 0; j < UNROLL; ++j) {
+                    uint64_t c = add63(x, y, p);
+                    x = y;
+                    y = c;
+                    if (c == 0)
+                        push(job.fb, idx + i + j + 1, p);
+                }
+            }
+        }
+    }
+    for (; i < steps; ++i) {
+        uint64_t c = addmod(a, b, p);
+        a = b;
+        b = c;
+        if (c == 0)
+            push(job.fb, idx + i + 1, p);
+    }
+}
+
+// (T(n), T(n+1), T(n+2)) mod p in Montgomery form by the doubling identities
+// T(2j)   = 2T(j+2)T(j) + T(j+1)^2 - 2T(j+1)T(j) - T(j)^2
+// T(2j+1) = T(j)^2 + 2T(j+2)T(j+1) - T(j+1)^2
+// T(2j+2) = 2T(j+1)T(j) + T(j+2)^2 + T(j+1)^2
+// (the formula section of OEIS A000073, as tribonacci.hpp:499-551 uses).
+__device__ __forceinline__ void trib_triple(const Mont &m, uint64_t n, uint64_t &t0, uint64_t &t1, uint64_t &t2)
+{
+    uint64_t x = 0, y = 0, z = m.one;
+    for (int bit = 63 - (n ? __clzll(n) : 63); n && bit >= 0; --bit) {
+        uint64_t xx = m.mul(x, x), yy = m.mul(y, y);
+        uint64_t xy2 = m.mul(m.dbl(y), x);
+        uint64_t nx = m.sub(m.sub(m.add(m.mul(m.dbl(z), x), yy), xy2), xx);
+        uint64_t ny = m.sub(m.add(xx, m.mul(m.dbl(z), y)), yy);
+        uint64_t nz = m.add(m.add(xy2, m.mul(z, z)), yy);
+        x = nx;
+        y = ny;
+        z = nz;
+        if ((n >> bit) & 1) {
+            uint64_t w = m.add(m.add(x, y), z);
+            x = y;
+            y = z;
+            z = w;
+        }
+    }
+    t0 = x;
+    t1 = y;
+    t2 = z;
+}
+
+// Tribonacci: state (T(n), T(n+1), T(n+2)), two addmods per step
+// (tribonacci.hpp:566-590).
+__device__ __forceinline__ void run_tribonacci(const JobView &job, uint64_t p, uint64_t s, uint64_t e)
+{
+    Mont m;
+    m.init(p);
+    uint64_t X, Y, Z;
+    trib_triple(m, s, X, Y, Z);
+    uint64_t x = m.from(X), y = m.from(Y), z = m.from(Z);
+    uint64_t idx = s - job.n0;
+    const uint64_t steps = e - s - 1;
+    if (x == 0)
+        push(job.fb, idx, p);
+    uint64_t i = 0;
+    if (p < (1ull << 62)) {
+        for (; i + UNROLL <= steps; i += UNROLL) {
+            const uint64_t x0 = x, y0 = y, z0 = z;
+            bool cand = false;
+#pragma unroll
+            for (int j = 0; j < UNROLL; ++j) {
+                uint64_t w = add63(add63(x, y, p), z, p);
+                x = y;
+                y = z;
+                z = w;
+                cand |= ((uint32_t)x == 0u);
+            }
+            if (cand) {
+                uint64_t a = x0, b = y0, c = z0;
+#pragma unroll 1
+                for (int j = 0; j < UNROLL; ++j) {
+                    uint64_t w = add63(add63(a, b, p), c, p);
+                    a = b;
+                    b = c;
+                    c = w;
+                    if (a == 0)
+                        push(job.fb, idx + i + j + 1, p);
+                }
+            }
+        }
+    }
+    for (; i < steps; ++i) {
+        uint64_t w = addmod(addmod(x, y, p), z, p);
+        x = y;
+        y = z;
+        z = w;
+        if (x == 0)
+            push(job.fb, idx + i + 1, p);
+    }
+}
+
+// ----------------------------------------------------------- Smarandache
+// Sm_b(n) = Sm_b(n-1) * b^len(n) + n (smarandache.hpp:131-198).  Within a
+// digit class (all m = n+1 with the same length d) the step is the affine
+// map x -> M x + m with M = b^d, so t steps from (x, m = c0) give
+//   x_t = M^t x + c0 G(t) + H(t),  G(t) = sum_{j<t} M^j,  H(t) = sum_{i<t} i M^(t-1-i)
+// with G(2t) = G(t)(1 + M^t), H(2t) = M^t H(t) + t G(t) + H(t),
+//      G(t+1) = M G(t) + 1,     H(t+1) = M H(t) + t.
+// This jump replaces the reference's reduction of the multi-limb Sm_b(n0)
+// (src/trial_factoring.cuh:197-202) and costs O(log n) per digit class.
+
+// smallest power of b above m (the end of m's digit class), saturating
+__device__ __forceinline__ uint64_t class_end(uint64_t b, uint64_t m, uint64_t &pw)
+{
+    pw = b;
+    while (pw <= m) {
+        if (pw > ~0ull / b) {
+            pw = ~0ull;
+            return pw;
+        }
+        pw *= b;
+    }
+    return pw;
+}
+
+// X (Montgomery form) -> after the steps m = c0 .. c0+t-1 with multiplier Mm (Montgomery form)
+__device__ __forceinline__ uint64_t affine_jump(const Mont &m, uint64_t X, uint64_t Mm, uint64_t c0, uint64_t t)
+{
+    if (!t)
+        return X;
+    uint64_t Mt = m.one, G = 0, H = 0, tc = 0;
+    for (int bit = 63 - __clzll(t); bit >= 0; --bit) {
+        if (tc) {
+            uint64_t tR = m.to(tc);
+            uint64_t H2 = m.add(m.add(m.mul(Mt, H), m.mul(tR, G)), H);
+            G = m.mul(G, m.add(m.one, Mt));
+            Mt = m.mul(Mt, Mt);
+            H = H2;
+            tc <<= 1;
+        }
+        if ((t >> bit) & 1) {
+            uint64_t tR = m.to(tc);
+            H = m.add(m.mul(Mm, H), tR);
+            G = m.add(m.mul(Mm, G), m.one);
+            Mt = m.mul(Mm, Mt);
+            tc += 1;
+        }
+    }
+    return m.add(m.add(m.mul(Mt, X), m.mul(m.to(c0), G)), H);
+}
+
+// Sm_b(s) mod p in Montgomery form, from Sm_b(0) = 0 class by class.
+__device__ __forceinline__ uint64_t smarandache_at(const Mont &m, uint64_t b, uint64_t s)
+{
+    uint64_t X = 0;
+    uint64_t c = 1;  // next m to apply
+    while (c <= s) {
+        uint64_t pw;
+        uint64_t cend = class_end(b, c, pw);  // M = pw for m in [c, cend)
+        uint64_t last = cend - 1 < s ? cend - 1 : s;
+        X = affine_jump(m, X, m.to(pw), c, last - c + 1);
+        c = last + 1;
+        if (cend == ~0ull)
+            break;
+    }
+    return X;
+}
+
+__device__ __forceinline__ void run_smarandache(const JobView &job, uint64_t p, uint64_t s, uint64_t e)
+{
+    const uint64_t b = job.param;
+    Mont m;
+    m.init(p);
+    uint64_t X = smarandache_at(m, b, s);
+    uint64_t idx0 = s - job.n0;
+    if (X == 0)
+        push(job.fb, idx0, p);
+    uint64_t mcur = s + 1;  // m = n + 1 of the next step
+    if (p < (1u << 30) && p >= e && e <= 0xffffffffull) {
+        // 32-bit Shoup path: x kept in [0, 3p) (Shoup output < 2p, plus m < p),
+        // so x = 0 mod p <=> x == p or x == 2p (x >= 1 after a step).
+        const uint32_t p32 = (uint32_t)p, p2 = 2 * p32;
+        uint32_t x = (uint32_t)m.from(X);
+        while (mcur < e) {
+            uint64_t pw;
+            uint64_t cend = class_end(b, mcur, pw);
+            const uint32_t M = (uint32_t)(pw % p);
+            const uint32_t Ms = shoup_precompute32(M, p32);
+            uint32_t mm = (uint32_t)mcur;
+            const uint32_t mend = (uint32_t)(cend < e ? cend : e);
+            while (mm + UNROLL <= mend) {
+                const uint32_t x0 = x;
+                bool cand = false;
+#pragma unroll
+                for (int j = 0; j < UNROLL; ++j) {
+                    uint32_t q = mulhi32(x, Ms);
+                    x = x * M + (mm + j) - q * p32;
+                    cand |= (x == p32) | (x == p2);
+                }
+                if (cand) {
+                    uint32_t y = x0;
+#pragma unroll 1
+                    for (int j = 0; j < UNROLL; ++j) {
+                        uint32_t q = mulhi32(y, Ms);
+                        y = y * M + (mm + j) - q * p32;
+                        if (y == p32 || y == p2)
+                            push(job.fb, (mm + j) - job.n0, p);
+                    }
+                }
+                mm += UNROLL;
+            }
+            for (; mm < mend; ++mm) {
+                uint32_t q = mulhi32(x, Ms);
+                x = x * M + mm - q * p32;
+                if (x == p32 || x == p2)
+                    push(job.fb, mm - job.n0, p);
+            }
+            mcur = mend;
+        }
+        return;
+    }
+    // general path: Montgomery form, X' = X * (M R) + m R
+    const uint64_t Rm = m.one;
+    uint64_t C = m.to(mcur);
+    while (mcur < e) {
+        uint64_t pw;
+        uint64_t cend = class_end(b, mcur, pw);
+        const uint64_t Mm = m.to(pw);
+        const uint64_t mend = cend < e ? cend : e;
+        for (; mcur < mend; ++mcur) {
+            X = m.add(m.mul(X, Mm), C);
+            C = m.add(C, Rm);
+            if (X == 0)
+                push(job.fb, mcur - job.n0, p);
+        }
+    }
+}
+
+// Peano S(n) = n, the reference's engine test sequence (tests/peano.hpp).
+__device__ __forceinline__ void run_peano(const JobView &job, uint64_t p, uint64_t s, uint64_t e)
+{
+    uint64_t r = s % p;
+    for (uint64_t n = s;; ++n) {
+        if (r == 0)
+            push(job.fb, n - job.n0, p);
+        if (n + 1 >= e)
+            break;
+        r = (r + 1 == p) ? 0 : r + 1;
+    }
+}
+
+template <uint32_t FAM>
+__device__ __forceinline__ void run_item(const JobView &job, uint64_t p, uint64_t s, uint64_t e)
+{
+    if (FAM == PROTH || FAM == RIESEL || FAM == MERSENNE)
+        run_doubling<FAM>(job, p, s, e);
+    else if (FAM == PROTH_FIXED_N || FAM == RIESEL_FIXED_N)
+        run_fixed_n<FAM>(job, p, s, e);
+    else if (FAM == FIBONACCI || FAM == LUCAS)
+        run_fibonacci<FAM>(job, p, s, e);
+    else if (FAM == TRIBONACCI)
+        run_tribonacci(job, p, s, e);
+    else if (FAM == SMARANDACHE)
+        run_smarandache(job, p, s, e);
+    else
+        run_peano(job, p, s, e);
+}
+
+template <uint32_t FAM>
+__global__ void __launch_bounds__(256) residue_kernel(JobView job, const uint64_t *__restrict__ primes, uint64_t nprimes)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t first = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (job.tiles == 1) {
+        for (uint64_t i = first; i < nprimes; i += stride)
+            run_item<FAM>(job, primes[i], job.n0, job.n1);
+        return;
+    }
+    const uint64_t items = nprimes * job.tiles;
+    for (uint64_t w = first; w < items; w += stride) {
+        uint64_t i = w / job.tiles;
+        uint64_t t = w - i * job.tiles;
+        uint64_t s = job.n0 + t * job.tile_len;
+        uint64_t e = s + job.tile_len < job.n1 ? s + job.tile_len : job.n1;
+        if (s < e)
+            run_item<FAM>(job, primes[i], s, e);
+    }
+}
+
+// --------------------------------------------------------- the prime 2
+// value_mod_2 / next_value_mod_2 of each family (number_sequence_helpers.hpp:14-37
+// and the per-family closed forms cited in the oracle).
+__device__ __forceinline__ uint64_t value_mod_2(uint32_t fam, uint64_t param, uint64_t n)
+{
+    switch (fam) {
+    case MERSENNE: return n > 0;
+    case PROTH:
+    case RIESEL: return n > 0 ? 1 : ((param & 1) ^ 1);
+    case SMARANDACHE: return (param & 1) ? (uint64_t)((n & 3) && ((n & 3) != 3)) : (n & 1);
+    case FIBONACCI:
+    case LUCAS: return n % 3 == 0 ? 0 : 1;
+    case PROTH_FIXED_N:
+    case RIESEL_FIXED_N: return 1;
+    case TRIBONACCI: return (n & 3) >> 1;
+    default: return n & 1;
+    }
+}
+
+__device__ __forceinline__ uint64_t next_value_mod_2(uint32_t fam, uint64_t param, uint64_t r, uint64_t n)
+{
+    switch (fam) {
+    case SMARANDACHE: return (param & 1) ? (r ^ (n & 1) ^ 1) : ((n & 1) ^ 1);
+    case FIBONACCI:
+    case LUCAS: return (n + 1) % 3 == 0 ? 0 : 1;
+    case TRIBONACCI: return ((n + 1) & 3) >> 1;
+    case CTD_PEANO: return r ^ 1;
+    default: return 1;
+    }
+}
+
+__global__ void mod2_kernel(JobView job)
+{
+    uint64_t r = value_mod_2(job.family, job.param, job.n0);
+    if (!r)
+        push(job.fb, 0, 2);
+    for (uint64_t n = job.n0; n + 1 < job.n1; ++n) {
+        r = next_value_mod_2(job.family, job.param, r, n);
+        if (!r)
+            push(job.fb, n + 1 - job.n0, 2);
+    }
+}
+
+// ----------------------------------------------------------- launchers
+template <uint32_t FAM>
+static cudaError_t launch_fam(const JobView &v, const uint64_t *d_primes, uint64_t n, int grid, int block,
+                              cudaStream_t st)
+{
+    residue_kernel<FAM><<<grid, block, 0, st>>>(v, d_primes, n);
+    return cudaGetLastError();
+}
+
+int launch_residues(const JobView &view, const uint64_t *d_primes, uint64_t nprimes, int grid, int block,
+                    cudaStream_t stream, std::string &err)
+{
+    if (!nprimes || view.n1 <= view.n0)
+        return CTD_OK;
+    cudaError_t rc;
+    switch (view.family) {
+    case MERSENNE: rc = launch_fam<MERSENNE>(view, d_primes, nprimes, grid, block, stream); break;
+    case PROTH: rc = launch_fam<PROTH>(view, d_primes, nprimes, grid, block, stream); break;
+    case RIESEL: rc = launch_fam<RIESEL>(view, d_primes, nprimes, grid, block, stream); break;
+    case SMARANDACHE: rc = launch_fam<SMARANDACHE>(view, d_primes, nprimes, grid, block, stream); break;
+    case FIBONACCI: rc = launch_fam<FIBONACCI>(view, d_primes, nprimes, grid, block, stream); break;
+    case LUCAS: rc = launch_fam<LUCAS>(view, d_primes, nprimes, grid, block, stream); break;
+    case PROTH_FIXED_N: rc = launch_fam<PROTH_FIXED_N>(view, d_primes, nprimes, grid, block, stream); break;
+    case RIESEL_FIXED_N: rc = launch_fam<RIESEL_FIXED_N>(view, d_primes, nprimes, grid, block, stream); break;
+    case TRIBONACCI: rc = launch_fam<TRIBONACCI>(view, d_primes, nprimes, grid, block, stream); break;
+    case PEANO: rc = launch_fam<PEANO>(view, d_primes, nprimes, grid, block, stream); break;
+    default: err = "unknown sequence family"; return CTD_ERR_INVALID_ARGUMENT;
+    }
+    if (rc != cudaSuccess) {
+        err = std::string("residue kernel launch: ") + cudaGetErrorString(rc);
+        return CTD_ERR_CUDA;
+    }
+    note_kernel_launch();
+    return CTD_OK;
+}
+
+int launch_mod2(const JobView &view, cudaStream_t stream, std::string &err)
+{
+    if (view.n1 <= view.n0)
+        return CTD_OK;
+    mod2_kernel<<<1, 1, 0, stream>>>(view);
+    cudaError_t rc = cudaGetLastError();
+    if (rc != cudaSuccess) {
+        err = std::string("mod-2 kernel launch: ") + cudaGetErrorString(rc);
+        return CTD_ERR_CUDA;
+    }
+    note_kernel_launch();
+    return CTD_OK;
+}
+
+}  // namespace ctd

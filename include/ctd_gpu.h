@@ -1,0 +1,157 @@
+/*
+ * ctd_gpu.h -- C ABI of libctd_gpu.so, the GB300 (sm_103a) trial-factoring
+ * engine for recurrence-defined integer sequences.
+ *
+ * Plain pointers and sizes only; no C++ or CUDA types cross this boundary
+ * (streams are passed as opaque `void *`, 0 meaning the context's own
+ * stream).  Every call returns an int status: CTD_OK (0) or a negative
+ * CTD_ERR_* code; ctd_last_error() gives the message of the last failure on
+ * a context.  No call throws.
+ *
+ * Each entry point names the reference interface it replaces (paths within
+ * the cutrialdive project).
+ */
+#ifndef CTD_GPU_H
+#define CTD_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CTD_ABI_VERSION 1
+
+/* ---- status codes ---- */
+#define CTD_OK 0
+#define CTD_ERR_INVALID_ARGUMENT (-1) /* bad job/range/pointer (reference: std::invalid_argument / runtime_error) */
+#define CTD_ERR_CUDA (-2)             /* a CUDA runtime call failed */
+#define CTD_ERR_OUT_OF_MEMORY (-3)    /* device allocation failed or a budget was exceeded */
+#define CTD_ERR_ABORTED (-4)          /* a progress callback asked to stop */
+#define CTD_ERR_TIMEOUT (-5)          /* a bounded device or host wait expired */
+#define CTD_ERR_CAPACITY (-6)         /* an output buffer is too small */
+#define CTD_ERR_NOT_FOUND (-7)        /* unknown job/request id */
+
+/* ---- sequence families: the numbering of num_seq_id (src/num_seq_id.hpp:16-26),
+ *      which the checkpoint file stores (src/checkpoint.cpp:186,213-216) ---- */
+#define CTD_MERSENNE 0
+#define CTD_PROTH 1
+#define CTD_RIESEL 2
+#define CTD_SMARANDACHE 3
+#define CTD_FIBONACCI 4
+#define CTD_LUCAS 5
+#define CTD_PROTH_FIXED_N 6
+#define CTD_RIESEL_FIXED_N 7
+#define CTD_TRIBONACCI 8
+/* S(n) = n, the reference's test-only sequence (tests/peano.hpp:127-137) */
+#define CTD_PEANO 256
+
+/*
+ * One trial-factoring job: the terms S(n), n in [n0, n1), of `family`
+ * (parameter `param`: k for proth/riesel, n for the fixed-n families, the
+ * base 2..64 for smarandache, unused otherwise) by every prime p in
+ * [f0, f1).  The device-side replacement of the template instantiation
+ * trial_factor<Seq>(trial_factoring_context&&, args...)
+ * (src/trial_factoring_impl.hpp:369-441) with its trial_factoring_options
+ * (src/trial_factoring_options.hpp:15-31).
+ */
+typedef struct ctd_job {
+    uint32_t family;
+    uint32_t max_factors; /* factors stored per term (--max-factors-per-number, default 32) */
+    uint64_t param;
+    uint64_t n0, n1;
+    uint64_t f0, f1;
+} ctd_job;
+
+/* Progress report after each completed prime segment. */
+typedef struct ctd_progress {
+    uint64_t segment_end;   /* upper bound fy of the segment just completed */
+    uint64_t last_prime;    /* largest prime processed so far, 0 if none */
+    uint64_t primes_done;   /* odd primes processed by this call so far */
+    double elapsed_s;       /* wall time since the call started */
+} ctd_progress;
+
+/* Return values of a progress callback. */
+#define CTD_CB_CONTINUE 0
+#define CTD_CB_SNAPSHOT 1 /* copy the factors buffer into the caller's arrays, then call back with snapshot=1 */
+#define CTD_CB_ABORT 2
+
+/* Called on the calling thread between segments (never while a kernel of
+ * this call runs).  With snapshot=1 the caller's counts/factors arrays hold
+ * the state after `prog->last_prime`: what the reference checkpoints
+ * (src/trial_factoring.cuh:453-465). */
+typedef int (*ctd_progress_cb)(void *user, const ctd_progress *prog, int snapshot);
+
+typedef struct ctd_ctx ctd_ctx;
+
+/* ---- library ---- */
+int ctd_abi_version(void);
+const char *ctd_strerror(int status);
+/* Number of kernels this process has launched through the library. */
+uint64_t ctd_kernel_launches(void);
+
+/* Opens a context on `device`.  Replaces cudaSetDevice + device property and
+ * occupancy queries of device_trial_factor (src/trial_factoring.cuh:342-380). */
+int ctd_open(int device, ctd_ctx **out);
+void ctd_close(ctd_ctx *ctx);
+const char *ctd_last_error(const ctd_ctx *ctx);
+/* Device name / memory / SM count (src/trial_factoring.cuh:241-252). */
+int ctd_device_info(ctd_ctx *ctx, char *name, size_t name_len, uint64_t *total_mem, int *sm_count);
+/* Override the residue kernel's launch shape (--grid-size / --block-size,
+ * src/trial_factoring.cuh:280-286); 0 restores the default. */
+int ctd_set_launch(ctd_ctx *ctx, int grid_size, int block_size);
+
+/* Validates a job like the reference's dispatch and range checks
+ * (src/num_seq_dispatch.hpp:120-170, src/trial_factoring_impl.hpp:380-387):
+ * CTD_OK, or CTD_ERR_INVALID_ARGUMENT. */
+int ctd_check_job(const ctd_job *job);
+
+/*
+ * Runs one job end to end on the device: the prime 2, then odd primes
+ * segment by segment (device sieve -> residue kernel), results merged into
+ * the caller-owned host factors buffer.  Replaces device_trial_factor
+ * (src/trial_factoring.cuh:334-513) and the kernels it launches
+ * (trial_div_by_2 :139-154, trial_div_by_odd_primes :156-228), including the
+ * host siever and its H2D prime copy (src/siever.hpp:179-237,
+ * src/prime_data.hpp:166-196).
+ *
+ * counts_inout[n1-n0] and factors_inout[(n1-n0)*max_factors] use the
+ * reference factors_buffer layout (src/factors_buffer.hpp:77-86); on entry
+ * they hold the resume state (zeros for a fresh job), on return the result
+ * (slot order is arrival order: sort per term before printing, as
+ * src/factors_buffer.hpp:123-138 does).  Primes p <= resume_after_prime are
+ * skipped (src/trial_factoring.cuh:404).  segment_length 0 = default 2^26.
+ */
+int ctd_run_plain(ctd_ctx *ctx, const ctd_job *job, uint32_t *counts_inout, uint64_t *factors_inout,
+                  uint64_t resume_after_prime, uint64_t segment_length, ctd_progress_cb cb, void *user);
+
+/*
+ * Primes in [lo, hi), ascending, from the device sieve, into a host array.
+ * *count receives the number of primes in the range; if it exceeds
+ * `capacity` the array holds the first `capacity` and CTD_ERR_CAPACITY is
+ * returned.  Replaces siever_impl::sieve (src/siever.hpp:179-237, primes in
+ * [start, end)).
+ */
+int ctd_sieve(ctd_ctx *ctx, uint64_t lo, uint64_t hi, uint64_t *out, uint64_t capacity, uint64_t *count);
+
+/* ---- device-resident forms (inputs and outputs in device memory) ---- */
+
+/* ctd_sieve into device memory, queued on `stream`. */
+int ctd_sieve_device(ctd_ctx *ctx, uint64_t lo, uint64_t hi, uint64_t *d_out, uint64_t capacity,
+                     uint64_t *count, void *stream);
+
+/* The residue kernel over an explicit list of odd primes in device memory,
+ * pushing hits into a device factors buffer.  The unit that
+ * trial_div_by_odd_primes<Seq, 1, ...> implements (src/trial_factoring.cuh:156-228).
+ * Asynchronous on `stream`. */
+int ctd_residues_device(ctd_ctx *ctx, const ctd_job *job, const uint64_t *d_primes, uint64_t nprimes,
+                        uint32_t *d_counts, uint64_t *d_factors, void *stream);
+
+/* The prime-2 pass into a device factors buffer (src/trial_factoring.cuh:139-154). */
+int ctd_mod2_device(ctd_ctx *ctx, const ctd_job *job, uint32_t *d_counts, uint64_t *d_factors, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
