@@ -26,7 +26,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2"
 
 CU_SOURCES = ["ctd_residue.cu", "ctd_sieve.cu", "ctd_engine.cu"]
 HEADERS = ["ctd_arith.cuh", "ctd_internal.h"]
-CLI_SOURCES = ["cli/main.cpp", "cli/command_line.cpp", "cli/checkpoint.cpp", "cli/results.cpp"]
+CLI_SOURCES = ["cli/main.cpp", "cli/command_line.cpp", "cli/results.cpp"]
 
 
 def nvcc() -> str:
