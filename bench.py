@@ -359,14 +359,19 @@ def run_ours(args, world, rank, local):
 
 
 def main() -> int:
+    global SEG, NSEG
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=NSEG)
+    ap.add_argument("--steps", type=int, default=NSEG, help="steps (default: every 2^30 segment once)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--segment-bits", type=int, default=30,
+                    help="log2 of the prime-segment width of one step (profiling uses smaller cases)")
     args = ap.parse_args()
+    SEG = 1 << args.segment_bits
+    NSEG = (F1 - F0) // SEG
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     world, rank, local = dist_env()

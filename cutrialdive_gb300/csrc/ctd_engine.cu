@@ -106,13 +106,14 @@ bool job_ok(const ctd_job *job)
 
 int default_block(const ctd_ctx *ctx) { return ctx->block_override > 0 ? ctx->block_override : 256; }
 
-int default_grid(const ctd_ctx *ctx, int block)
+int default_grid(ctd_ctx *ctx, uint32_t family, int block)
 {
     if (ctx->grid_override > 0)
         return ctx->grid_override;
-    // persistent-style grid: enough resident warps to hide the integer
-    // pipeline latency; the kernels stride over their work items
-    int per_sm = 2048 / block;
+    // persistent grid: exactly the CTAs that are resident at once, so every
+    // thread strides over the same number of work items and no CTA waits
+    // for a second wave
+    int per_sm = residue_blocks_per_sm(family, block);
     if (per_sm < 1)
         per_sm = 1;
     return ctx->sm_count * per_sm;
@@ -301,7 +302,7 @@ int ctd_residues_device(ctd_ctx *ctx, const ctd_job *job, const uint64_t *d_prim
     cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
     JobView v = make_view(job, d_counts, d_factors);
     const int block = default_block(ctx);
-    const int grid = default_grid(ctx, block);
+    const int grid = default_grid(ctx, job->family, block);
     choose_tiles(ctx, nprimes, job->n1 - job->n0, grid, block, v.tiles, v.tile_len);
     std::string err;
     int rc = launch_residues(v, d_primes, nprimes, grid, block, st, err);
@@ -356,7 +357,7 @@ int ctd_run_plain(ctd_ctx *ctx, const ctd_job *job, uint32_t *counts_inout, uint
     }
     const uint64_t seg = segment_length ? segment_length : (1ull << 26);
     const int block = default_block(ctx);
-    const int grid = default_grid(ctx, block);
+    const int grid = default_grid(ctx, job->family, block);
     uint64_t last_prime = resume_after_prime;
     uint64_t primes_done = 0;
     for (uint64_t fx = f0, fy = (f1 - f0 > seg) ? f0 + seg : f1; fx < f1;

@@ -72,6 +72,9 @@ uint64_t prime_count_upper_bound(uint64_t lo, uint64_t hi);
 // nprimes x view.tiles work items.
 int launch_residues(const JobView &view, const uint64_t *d_primes, uint64_t nprimes, int grid, int block,
                     cudaStream_t stream, std::string &err);
+// Resident CTAs per SM of the family's residue kernel at `block` threads
+// (0 if the query fails); the persistent grid is SMs x this.
+int residue_blocks_per_sm(uint32_t family, int block);
 // The prime 2: the reference's serial mod-2 pass (src/trial_factoring.cuh:139-154).
 int launch_mod2(const JobView &view, cudaStream_t stream, std::string &err);
 // Number of kernel launches issued by this process so far (diagnostics).

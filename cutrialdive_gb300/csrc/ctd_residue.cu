@@ -40,18 +40,59 @@ __device__ __forceinline__ void push(const FactorsView &fb, uint64_t idx, uint64
 }
 
 // ------------------------------------------------------- step primitives
-// 2u mod p and u + c mod p for p < 2^63: one wrapped subtraction and a sign
-// test instead of a compare-and-select on the unreduced value.
-__device__ __forceinline__ uint64_t dbl63(uint64_t u, uint64_t p)
+// For p < 2^63 the modular double / add is: v = a + b - p (one 3-input add
+// pair), then v += p under the sign of v (a predicated add pair) -- five
+// 32-bit integer instructions, no compare-and-select on the unreduced value.
+__device__ __forceinline__ uint64_t add63(uint64_t a, uint64_t b, uint64_t p)
 {
-    uint64_t v = (u << 1) - p;
-    return ((int64_t)v < 0) ? v + p : v;
+    uint64_t v;
+    asm("{\n\t.reg .pred neg;\n\t"
+        "add.u64 %0, %1, %2;\n\t"
+        "sub.u64 %0, %0, %3;\n\t"
+        "setp.lt.s64 neg, %0, 0;\n\t"
+        "@neg add.u64 %0, %0, %3;\n\t"
+        "}"
+        : "=l"(v)
+        : "l"(a), "l"(b), "l"(p));
+    return v;
 }
 
-__device__ __forceinline__ uint64_t add63(uint64_t u, uint64_t c, uint64_t p)
+__device__ __forceinline__ uint64_t dbl63(uint64_t u, uint64_t p) { return add63(u, u, p); }
+
+// One step of u <- u + c (c = u for doubling) with the candidate test folded
+// into the predicate `hit`: hit |= (low word of u == tlo).
+#define CTD_ADD_STEP(U, C, P, T)                 \
+    "add.u64 " U ", " U ", " C ";\n\t"           \
+    "sub.u64 " U ", " U ", " P ";\n\t"           \
+    "setp.lt.s64 neg, " U ", 0;\n\t"             \
+    "@neg add.u64 " U ", " U ", " P ";\n\t"      \
+    "mov.b64 {lo, hi}, " U ";\n\t"               \
+    "setp.eq.or.u32 hit, lo, " T ", hit;\n\t"
+
+// Eight steps of u <- u + c mod p (c == u: doubling) in one block of PTX;
+// returns whether any intermediate low word equalled `tlo`.
+template <bool DOUBLE>
+__device__ __forceinline__ uint32_t step8_add63(uint64_t &u, uint64_t c, uint64_t p, uint32_t tlo)
 {
-    uint64_t v = u + c - p;
-    return ((int64_t)v < 0) ? v + p : v;
+    uint32_t cand;
+    // operands: %0 = u, %1 = candidate flag, %2 = p, %3 = tlo, %4 = c
+#define CTD_S8(C)                                                                                   \
+    CTD_ADD_STEP("%0", C, "%2", "%3") CTD_ADD_STEP("%0", C, "%2", "%3") CTD_ADD_STEP("%0", C, "%2", "%3") \
+    CTD_ADD_STEP("%0", C, "%2", "%3") CTD_ADD_STEP("%0", C, "%2", "%3") CTD_ADD_STEP("%0", C, "%2", "%3") \
+    CTD_ADD_STEP("%0", C, "%2", "%3") CTD_ADD_STEP("%0", C, "%2", "%3")
+    if (DOUBLE) {
+        asm("{\n\t.reg .pred neg, hit;\n\t.reg .b32 lo, hi;\n\t"
+            "setp.ne.u32 hit, %3, %3;\n\t" CTD_S8("%0") "selp.u32 %1, 1, 0, hit;\n\t}"
+            : "+l"(u), "=r"(cand)
+            : "l"(p), "r"(tlo), "l"(c));
+    } else {
+        asm("{\n\t.reg .pred neg, hit;\n\t.reg .b32 lo, hi;\n\t"
+            "setp.ne.u32 hit, %3, %3;\n\t" CTD_S8("%4") "selp.u32 %1, 1, 0, hit;\n\t}"
+            : "+l"(u), "=r"(cand)
+            : "l"(p), "r"(tlo), "l"(c));
+    }
+#undef CTD_S8
+    return cand;
 }
 
 constexpr int UNROLL = 8;
@@ -92,6 +133,35 @@ __device__ __forceinline__ void walk_target(uint64_t u, uint64_t target, uint64_
     }
 }
 
+// walk_target for u <- u + c (DOUBLE: u <- 2u) with p < 2^63, blocks of
+// eight steps in PTX with the candidate predicate kept across the block.
+template <bool DOUBLE>
+__device__ __forceinline__ void walk_add63(uint64_t u, uint64_t c, uint64_t target, uint64_t p, uint64_t idx,
+                                           uint64_t steps, const FactorsView &fb)
+{
+    if (u == target)
+        push(fb, idx, p);
+    const uint32_t tlo = (uint32_t)target;
+    uint64_t i = 0;
+    for (; i + UNROLL <= steps; i += UNROLL) {
+        const uint64_t u0 = u;
+        if (step8_add63<DOUBLE>(u, c, p, tlo)) {
+            uint64_t v = u0;
+#pragma unroll 1
+            for (int j = 0; j < UNROLL; ++j) {
+                v = DOUBLE ? add63(v, v, p) : add63(v, c, p);
+                if (v == target)
+                    push(fb, idx + i + j + 1, p);
+            }
+        }
+    }
+    for (; i < steps; ++i) {
+        u = DOUBLE ? add63(u, u, p) : add63(u, c, p);
+        if (u == target)
+            push(fb, idx + i + 1, p);
+    }
+}
+
 // ------------------------------------------------------------- families
 
 // Proth k*2^n+1, Riesel k*2^n-1, Mersenne 2^n-1 (riesel_proth.hpp:90-115,
@@ -110,7 +180,7 @@ __device__ __forceinline__ void run_doubling(const JobView &job, uint64_t p, uin
     const uint64_t target = (FAM == PROTH) ? p - 1 : 1;
     const uint64_t steps = e - s - 1;
     if (p < (1ull << 63))
-        walk_target(u, target, p, s - job.n0, steps, job.fb, [p](uint64_t x) { return dbl63(x, p); });
+        walk_add63<true>(u, 0, target, p, s - job.n0, steps, job.fb);
     else
         walk_target(u, target, p, s - job.n0, steps, job.fb, [p](uint64_t x) { return dblmod(x, p); });
 }
@@ -129,7 +199,7 @@ __device__ __forceinline__ void run_fixed_n(const JobView &job, uint64_t p, uint
     const uint64_t target = (FAM == PROTH_FIXED_N) ? p - 1 : 1;
     const uint64_t steps = e - s - 1;
     if (p < (1ull << 63))
-        walk_target(v, target, p, s - job.n0, steps, job.fb, [p, c](uint64_t x) { return add63(x, c, p); });
+        walk_add63<false>(v, c, target, p, s - job.n0, steps, job.fb);
     else
         walk_target(v, target, p, s - job.n0, steps, job.fb, [p, c](uint64_t x) { return addmod(x, c, p); });
 }
@@ -184,16 +254,22 @@ __device__ __forceinline__ void run_fibonacci(const JobView &job, uint64_t p, ui
         push(job.fb, idx, p);
     uint64_t i = 0;
     if (p < (1ull << 63)) {
+        const uint32_t zero = 0;
         for (; i + UNROLL <= steps; i += UNROLL) {
             const uint64_t a0 = a, b0 = b;
-            bool cand = false;
-#pragma unroll
-            for (int j = 0; j < UNROLL; ++j) {
-                uint64_t c = add63(a, b, p);
-                a = b;
-                b = c;
-                cand |= ((uint32_t)c == 0u);
-            }
+            uint32_t cand;
+            // a <- a + b, b <- b + a alternately: (a, b) is (S(n-1), S(n))
+            // again after every second step, with no register moves
+            // operands: %0 = a, %1 = b, %2 = candidate flag, %3 = p, %4 = 0
+            asm("{\n\t.reg .pred neg, hit;\n\t.reg .b32 lo, hi;\n\t"
+                "setp.ne.u32 hit, %4, %4;\n\t"
+                CTD_ADD_STEP("%0", "%1", "%3", "%4") CTD_ADD_STEP("%1", "%0", "%3", "%4")
+                CTD_ADD_STEP("%0", "%1", "%3", "%4") CTD_ADD_STEP("%1", "%0", "%3", "%4")
+                CTD_ADD_STEP("%0", "%1", "%3", "%4") CTD_ADD_STEP("%1", "%0", "%3", "%4")
+                CTD_ADD_STEP("%0", "%1", "%3", "%4") CTD_ADD_STEP("%1", "%0", "%3", "%4")
+                "selp.u32 %2, 1, 0, hit;\n\t}"
+                : "+l"(a), "+l"(b), "=r"(cand)
+                : "l"(p), "r"(zero));
             if (cand) {
                 uint64_t x = a0, y = b0;
 #pragma unroll 1
@@ -245,8 +321,31 @@ __device__ __forceinline__ void trib_triple(const Mont &m, uint64_t n, uint64_t 
     t2 = z;
 }
 
+// x <- x + y + z mod p for x, y, z < p < 2^62: the sum minus 2p, then p
+// added back up to twice under the sign; the candidate test on the result.
+// operands of the tribonacci block: %0..%2 = x, y, z, %3 = candidate flag,
+// %4 = p, %5 = 2p, %6 = 0
+#define CTD_TRIB_STEP(X, Y, Z)                   \
+    "add.u64 " X ", " X ", " Y ";\n\t"           \
+    "add.u64 " X ", " X ", " Z ";\n\t"           \
+    "sub.u64 " X ", " X ", %5;\n\t"              \
+    "setp.lt.s64 neg, " X ", 0;\n\t"             \
+    "@neg add.u64 " X ", " X ", %4;\n\t"         \
+    "setp.lt.s64 neg, " X ", 0;\n\t"             \
+    "@neg add.u64 " X ", " X ", %4;\n\t"         \
+    "mov.b64 {lo, hi}, " X ";\n\t"               \
+    "setp.eq.or.u32 hit, lo, %6, hit;\n\t"
+
+__device__ __forceinline__ uint64_t trib_add(uint64_t x, uint64_t y, uint64_t z, uint64_t p)
+{
+    return addmod(addmod(x, y, p), z, p);
+}
+
 // Tribonacci: state (T(n), T(n+1), T(n+2)), two addmods per step
-// (tribonacci.hpp:566-590).
+// (tribonacci.hpp:566-590).  Each step computes T(n+3), which is the residue
+// of index n+3: the first three indices are tested from the jump, then every
+// new value at its own index, so the state rotates in place (x, y, z take
+// turns holding the newest value) and the steps need no register moves.
 __device__ __forceinline__ void run_tribonacci(const JobView &job, uint64_t p, uint64_t s, uint64_t e)
 {
     Mont m;
@@ -254,44 +353,52 @@ __device__ __forceinline__ void run_tribonacci(const JobView &job, uint64_t p, u
     uint64_t X, Y, Z;
     trib_triple(m, s, X, Y, Z);
     uint64_t x = m.from(X), y = m.from(Y), z = m.from(Z);
-    uint64_t idx = s - job.n0;
-    const uint64_t steps = e - s - 1;
-    if (x == 0)
-        push(job.fb, idx, p);
-    uint64_t i = 0;
+    const uint64_t idx = s - job.n0;
+    const uint64_t len = e - s;
+    const uint64_t first[3] = {x, y, z};
+    for (uint64_t j = 0; j < 3 && j < len; ++j)
+        if (first[j] == 0)
+            push(job.fb, idx + j, p);
+    if (len <= 3)
+        return;
+    const uint64_t steps = len - 3;  // values T(s+3) .. T(e-1)
+    uint64_t i = 0;                   // value T(s+3+i) goes to index idx+3+i
     if (p < (1ull << 62)) {
-        for (; i + UNROLL <= steps; i += UNROLL) {
+        constexpr int TB = 6;
+        const uint32_t zero = 0;
+        const uint64_t p2 = 2 * p;
+        for (; i + TB <= steps; i += TB) {
             const uint64_t x0 = x, y0 = y, z0 = z;
-            bool cand = false;
-#pragma unroll
-            for (int j = 0; j < UNROLL; ++j) {
-                uint64_t w = add63(add63(x, y, p), z, p);
-                x = y;
-                y = z;
-                z = w;
-                cand |= ((uint32_t)x == 0u);
-            }
+            uint32_t cand;
+            asm("{\n\t.reg .pred neg, hit;\n\t.reg .b32 lo, hi;\n\t"
+                "setp.ne.u32 hit, %6, %6;\n\t"
+                CTD_TRIB_STEP("%0", "%1", "%2") CTD_TRIB_STEP("%1", "%2", "%0")
+                CTD_TRIB_STEP("%2", "%0", "%1") CTD_TRIB_STEP("%0", "%1", "%2")
+                CTD_TRIB_STEP("%1", "%2", "%0") CTD_TRIB_STEP("%2", "%0", "%1")
+                "selp.u32 %3, 1, 0, hit;\n\t}"
+                : "+l"(x), "+l"(y), "+l"(z), "=r"(cand)
+                : "l"(p), "l"(p2), "r"(zero));
             if (cand) {
                 uint64_t a = x0, b = y0, c = z0;
 #pragma unroll 1
-                for (int j = 0; j < UNROLL; ++j) {
-                    uint64_t w = add63(add63(a, b, p), c, p);
+                for (int j = 0; j < TB; ++j) {
+                    uint64_t w = trib_add(a, b, c, p);
                     a = b;
                     b = c;
                     c = w;
-                    if (a == 0)
-                        push(job.fb, idx + i + j + 1, p);
+                    if (w == 0)
+                        push(job.fb, idx + 3 + i + j, p);
                 }
             }
         }
     }
     for (; i < steps; ++i) {
-        uint64_t w = addmod(addmod(x, y, p), z, p);
+        uint64_t w = trib_add(x, y, z, p);
         x = y;
         y = z;
         z = w;
-        if (x == 0)
-            push(job.fb, idx + i + 1, p);
+        if (w == 0)
+            push(job.fb, idx + 3 + i, p);
     }
 }
 
@@ -560,6 +667,32 @@ int launch_residues(const JobView &view, const uint64_t *d_primes, uint64_t npri
     }
     note_kernel_launch();
     return CTD_OK;
+}
+
+template <uint32_t FAM>
+static int occupancy(int block)
+{
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, residue_kernel<FAM>, block, 0) != cudaSuccess)
+        return 0;
+    return n;
+}
+
+int residue_blocks_per_sm(uint32_t family, int block)
+{
+    switch (family) {
+    case MERSENNE: return occupancy<MERSENNE>(block);
+    case PROTH: return occupancy<PROTH>(block);
+    case RIESEL: return occupancy<RIESEL>(block);
+    case SMARANDACHE: return occupancy<SMARANDACHE>(block);
+    case FIBONACCI: return occupancy<FIBONACCI>(block);
+    case LUCAS: return occupancy<LUCAS>(block);
+    case PROTH_FIXED_N: return occupancy<PROTH_FIXED_N>(block);
+    case RIESEL_FIXED_N: return occupancy<RIESEL_FIXED_N>(block);
+    case TRIBONACCI: return occupancy<TRIBONACCI>(block);
+    case PEANO: return occupancy<PEANO>(block);
+    default: return 0;
+    }
 }
 
 int launch_mod2(const JobView &view, cudaStream_t stream, std::string &err)
