@@ -117,11 +117,12 @@ def test_cli_resume_from_checkpoint(tmp_path):
     opts = ctd.trial_factoring_options(1, 20001, 1 << 24, 1 << 27, str(part), 32)
     buf = ctd.factors_buffer.empty(1, 20000, 32)
     # the first three segments only
-    ctd.engine(0).run_plain(ctd.make_job(spec, ctd.trial_factoring_options(1, 20001, 1 << 24, 1 << 24 | 3 << 24)),
+    split = (1 << 24) + (3 << 24)
+    ctd.engine(0).run_plain(ctd.make_job(spec, ctd.trial_factoring_options(1, 20001, 1 << 24, split)),
                             buf, segment_length=1 << 24)
     import oracle
 
-    last = int(oracle.sieve((1 << 24) + (3 << 24) - 4096, (1 << 24) + (3 << 24))[-1])
+    last = int(oracle.sieve(split - 4096, split)[-1])
     ctd.write_checkpoint(str(part) + ".chkpnt", spec, opts, last, buf)
     r = cli("--resume", str(part) + ".chkpnt", "--no-progress", cwd=tmp_path)
     assert r.returncode == 0, r.stderr
