@@ -54,6 +54,7 @@ SIGNATURES = {
     "ctd_sieve_device": (i32, [vp, u64, u64, vp, u64, p64, vp]),
     "ctd_residues_device": (i32, [vp, ctypes.POINTER(CtdJob), vp, u64, vp, vp, vp]),
     "ctd_mod2_device": (i32, [vp, ctypes.POINTER(CtdJob), vp, vp, vp]),
+    "ctd_sieve_device_noalloc": (i32, [vp, u64, u64, vp, u64, p64, vp]),
 }
 
 _lib = None

@@ -158,6 +158,13 @@ JobView make_view(const ctd_job *job, uint32_t *d_counts, uint64_t *d_factors)
 
 }  // namespace
 
+namespace ctd {
+int ctx_device(const ctd_ctx *ctx) { return ctx->device; }
+int ctx_sm_count(const ctd_ctx *ctx) { return ctx->sm_count; }
+cudaStream_t ctx_stream(const ctd_ctx *ctx) { return ctx->stream; }
+int ctx_fail(ctd_ctx *ctx, int code, const std::string &msg) { return fail(ctx, code, msg); }
+}  // namespace ctd
+
 extern "C" {
 
 int ctd_abi_version(void) { return CTD_ABI_VERSION; }

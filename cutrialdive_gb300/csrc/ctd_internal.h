@@ -67,6 +67,32 @@ int sieve_range(SieveWorkspace *ws, uint64_t lo, uint64_t hi, uint64_t *d_out, u
 // Upper bound on the number of primes in [lo, hi) (for buffer sizing).
 uint64_t prime_count_upper_bound(uint64_t lo, uint64_t hi);
 
+// Geometry of a sieve window: 16384 words of 32 odd numbers (a 2^20-wide range).
+constexpr uint64_t SIEVE_WIN_WORDS = 16384;
+constexpr uint64_t SIEVE_WIN_RANGE = 2 * 32 * SIEVE_WIN_WORDS;
+constexpr uint32_t SIEVE_LEVEL0_ODD_PRIMES = 6541;  // odd primes below 2^16
+
+// Scratch for the fixed-scratch sieve (sieve_range_scratch): device pointers
+// the caller owns; bits/wcount/offsets hold `max_windows` windows.
+struct SieveScratch {
+    uint32_t *bits;
+    uint32_t *wcount;
+    uint64_t *offsets;
+    uint32_t *base;
+    uint64_t base_cap;
+    uint32_t *level0_count;
+    uint64_t max_windows;
+};
+// Windows the fixed-scratch sieve needs for [lo, hi), and for the base primes
+// up to `limit` above 2^16.
+uint64_t sieve_scratch_windows(uint64_t lo, uint64_t hi);
+uint64_t sieve_scratch_base_windows(uint64_t limit);
+// Primes in [lo, hi) using only `sc` as scratch: no allocation, no state
+// kept between calls (base primes recomputed).  Synchronizes `stream` once
+// to read the count.
+int sieve_range_scratch(const SieveScratch &sc, int sm_count, uint64_t lo, uint64_t hi, uint64_t *d_out,
+                        uint64_t capacity, uint64_t *count, cudaStream_t stream, std::string &err);
+
 // -------------------------------------------------------------- residues
 // Odd primes only.  Launches the family's residue kernel over
 // nprimes x view.tiles work items.
@@ -80,5 +106,11 @@ int launch_mod2(const JobView &view, cudaStream_t stream, std::string &err);
 // Number of kernel launches issued by this process so far (diagnostics).
 uint64_t kernel_launch_count();
 void note_kernel_launch();
+
+// Context accessors for entry points defined outside ctd_engine.cu.
+int ctx_device(const ctd_ctx *ctx);
+int ctx_sm_count(const ctd_ctx *ctx);
+cudaStream_t ctx_stream(const ctd_ctx *ctx);
+int ctx_fail(ctd_ctx *ctx, int code, const std::string &msg);
 
 }  // namespace ctd

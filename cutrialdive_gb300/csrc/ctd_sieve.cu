@@ -460,6 +460,92 @@ uint64_t prime_count_upper_bound(uint64_t lo, uint64_t hi)
     return (uint64_t)bound + 64;
 }
 
+// ----------------------------------------------- fixed-scratch variant
+// The same three-pass sieve over scratch the caller provides (no device
+// allocation, no cached state): base primes are recomputed on every call
+// into `sc.base`, whose unused tail is filled with 0xffffffff so the kernels'
+// "p^2 beyond the window" test stops at the real list.
+uint64_t sieve_scratch_windows(uint64_t lo, uint64_t hi)
+{
+    const uint64_t lo_odd = lo < 3 ? 3 : (lo | 1);
+    if (lo_odd >= hi)
+        return 0;
+    const uint64_t nodd = (hi - lo_odd + 1) / 2;
+    return (nodd + WIN_ODD - 1) / WIN_ODD;
+}
+
+uint64_t sieve_scratch_base_windows(uint64_t limit)
+{
+    return limit < LEVEL0_LIMIT ? 0 : (limit - LEVEL0_LIMIT) / (2 * WIN_ODD) + 1;
+}
+
+int sieve_range_scratch(const SieveScratch &sc, int sm_count, uint64_t lo, uint64_t hi, uint64_t *d_out,
+                        uint64_t capacity, uint64_t *count, cudaStream_t st, std::string &err)
+{
+    *count = 0;
+    if (hi <= lo)
+        return CTD_OK;
+    const size_t smem = WIN_WORDS * sizeof(uint32_t);
+    CUDA_TRY(cudaFuncSetAttribute(sieve_windows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    uint64_t out_base = 0;
+    if (lo <= 2 && hi > 2) {
+        if (capacity > 0) {  // the u64 value 2, little-endian
+            CUDA_TRY(cudaMemsetAsync(d_out, 0, sizeof(uint64_t), st));
+            CUDA_TRY(cudaMemsetAsync(d_out, 2, 1, st));
+        }
+        out_base = 1;
+    }
+    const uint64_t lo_odd = lo < 3 ? 3 : (lo | 1);
+    if (lo_odd >= hi) {
+        *count = out_base;
+        return CTD_OK;
+    }
+    // base primes: level 0 (odd p < 2^16), then (2^16, sqrt(hi)] from them
+    const uint64_t limit = isqrt64(hi - 1);
+    CUDA_TRY(cudaMemsetAsync(sc.base, 0xff, sc.base_cap * sizeof(uint32_t), st));
+    level0_primes<<<1, 1024, 0, st>>>(sc.base, sc.level0_count);
+    CUDA_TRY(cudaGetLastError());
+    note_kernel_launch();
+    const uint32_t nlevel0 = 6541;  // odd primes below 2^16
+    const uint64_t bwin = sieve_scratch_base_windows(limit);
+    if (bwin) {
+        const uint64_t b_lo = LEVEL0_LIMIT + 1;
+        const uint64_t b_nodd = (limit - b_lo) / 2 + 1;
+        const int grid = (int)std::min<uint64_t>(bwin, (uint64_t)sm_count * 3);
+        sieve_windows<<<grid, SIEVE_THREADS, smem, st>>>(b_lo, b_nodd, (uint32_t)bwin, sc.base, nlevel0, sc.bits,
+                                                         sc.wcount);
+        CUDA_TRY(cudaGetLastError());
+        scan_counts<<<1, 1024, 0, st>>>(sc.wcount, (uint32_t)bwin, sc.offsets);
+        CUDA_TRY(cudaGetLastError());
+        compact_windows<uint32_t><<<grid, SIEVE_THREADS, 0, st>>>(b_lo, (uint32_t)bwin, sc.bits, sc.offsets, sc.base,
+                                                                  sc.base_cap - 1, nlevel0);
+        CUDA_TRY(cudaGetLastError());
+        note_kernel_launch();
+        note_kernel_launch();
+        note_kernel_launch();
+    }
+    // the range itself, against every base prime (the sentinel tail stops the scan)
+    const uint64_t nodd = (hi - lo_odd + 1) / 2;
+    const uint64_t nwin = (nodd + WIN_ODD - 1) / WIN_ODD;
+    const int grid = (int)std::min<uint64_t>(nwin, (uint64_t)sm_count * 3);
+    sieve_windows<<<grid, SIEVE_THREADS, smem, st>>>(lo_odd, nodd, (uint32_t)nwin, sc.base, sc.base_cap, sc.bits,
+                                                     sc.wcount);
+    CUDA_TRY(cudaGetLastError());
+    scan_counts<<<1, 1024, 0, st>>>(sc.wcount, (uint32_t)nwin, sc.offsets);
+    CUDA_TRY(cudaGetLastError());
+    compact_windows<uint64_t><<<grid, SIEVE_THREADS, 0, st>>>(lo_odd, (uint32_t)nwin, sc.bits, sc.offsets, d_out,
+                                                              capacity, out_base);
+    CUDA_TRY(cudaGetLastError());
+    note_kernel_launch();
+    note_kernel_launch();
+    note_kernel_launch();
+    uint64_t total = 0;
+    CUDA_TRY(cudaMemcpyAsync(&total, sc.offsets + nwin, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    *count = out_base + total;
+    return CTD_OK;
+}
+
 int sieve_range(SieveWorkspace *ws, uint64_t lo, uint64_t hi, uint64_t *d_out, uint64_t capacity, uint64_t *count,
                 cudaStream_t st, std::string &err)
 {

@@ -151,6 +151,26 @@ int ctd_residues_device(ctd_ctx *ctx, const ctd_job *job, const uint64_t *d_prim
 /* The prime-2 pass into a device factors buffer (src/trial_factoring.cuh:139-154). */
 int ctd_mod2_device(ctd_ctx *ctx, const ctd_job *job, uint32_t *d_counts, uint64_t *d_factors, void *stream);
 
+/* ---- allocation-free device sieve ----
+ * No counterpart in the reference.  For callers that may not allocate device
+ * memory -- a process that reserves its whole memory budget at start-up and
+ * admits work against it, or a host whose pool allocator owns all GPU
+ * memory -- this is ctd_sieve_device without any cudaMalloc/cudaFree: its
+ * scratch is a fixed array of about 8.6 MiB compiled into the library, held
+ * on each GPU that loads the library until the process exits.  Limits:
+ * hi - lo <= CTD_NOALLOC_SIEVE_MAX_RANGE and hi <= CTD_NOALLOC_SIEVE_MAX_HI;
+ * larger requests return CTD_ERR_INVALID_ARGUMENT (message in
+ * ctd_last_error).  Output as ctd_sieve_device: primes in [lo, hi) ascending
+ * in the caller's d_out, *count the number of primes (synchronizes the
+ * stream to read it).  The first call on a device looks up the array's
+ * device address; make that first call before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU (concurrent streams or
+ * threads) race and must be serialized by the caller. */
+#define CTD_NOALLOC_SIEVE_MAX_RANGE (1ull << 26)
+#define CTD_NOALLOC_SIEVE_MAX_HI (1ull << 48)
+int ctd_sieve_device_noalloc(ctd_ctx *ctx, uint64_t lo, uint64_t hi, uint64_t *d_out, uint64_t capacity,
+                             uint64_t *count, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
