@@ -59,37 +59,44 @@ __device__ __forceinline__ uint64_t add63(uint64_t a, uint64_t b, uint64_t p)
 
 __device__ __forceinline__ uint64_t dbl63(uint64_t u, uint64_t p) { return add63(u, u, p); }
 
-// One step of u <- u + c (c = u for doubling) with the candidate test folded
-// into the predicate `hit`: hit |= (low word of u == tlo).
-#define CTD_ADD_STEP(U, C, P, T)                 \
+// One step of u <- u + c (c = u for doubling) with the candidate test on the
+// FMA pipe: acc *= (low word of u) - (low word of the target), so acc becomes
+// 0 when a low word matched (a product of nonzero words reaches 0 mod 2^32
+// only by accumulating 32 factors of two: rare false candidates, never a
+// missed one).  The integer ALU pipe, the kernel's bottleneck, is left with
+// the add pair, the sign test and the predicated add pair.
+#define CTD_ADD_STEP(U, C, P, NT)                \
     "add.u64 " U ", " U ", " C ";\n\t"           \
     "sub.u64 " U ", " U ", " P ";\n\t"           \
     "setp.lt.s64 neg, " U ", 0;\n\t"             \
     "@neg add.u64 " U ", " U ", " P ";\n\t"      \
     "mov.b64 {lo, hi}, " U ";\n\t"               \
-    "setp.eq.or.u32 hit, lo, " T ", hit;\n\t"
+    "mad.lo.u32 x, lo, 1, " NT ";\n\t"           \
+    "mul.lo.u32 acc, acc, x;\n\t"
+
+#define CTD_BLOCK_HEAD "{\n\t.reg .pred neg, hit;\n\t.reg .b32 lo, hi, x, acc;\n\tmov.u32 acc, 1;\n\t"
+#define CTD_BLOCK_TAIL(OUT) "setp.eq.u32 hit, acc, 0;\n\tselp.u32 " OUT ", 1, 0, hit;\n\t}"
 
 // Eight steps of u <- u + c mod p (c == u: doubling) in one block of PTX;
-// returns whether any intermediate low word equalled `tlo`.
+// returns nonzero when a low word may have equalled the target's
+// (ntlo = -(low word of the target)).
 template <bool DOUBLE>
-__device__ __forceinline__ uint32_t step8_add63(uint64_t &u, uint64_t c, uint64_t p, uint32_t tlo)
+__device__ __forceinline__ uint32_t step8_add63(uint64_t &u, uint64_t c, uint64_t p, uint32_t ntlo)
 {
     uint32_t cand;
-    // operands: %0 = u, %1 = candidate flag, %2 = p, %3 = tlo, %4 = c
+    // operands: %0 = u, %1 = candidate flag, %2 = p, %3 = ntlo, %4 = c
 #define CTD_S8(C)                                                                                   \
     CTD_ADD_STEP("%0", C, "%2", "%3") CTD_ADD_STEP("%0", C, "%2", "%3") CTD_ADD_STEP("%0", C, "%2", "%3") \
     CTD_ADD_STEP("%0", C, "%2", "%3") CTD_ADD_STEP("%0", C, "%2", "%3") CTD_ADD_STEP("%0", C, "%2", "%3") \
     CTD_ADD_STEP("%0", C, "%2", "%3") CTD_ADD_STEP("%0", C, "%2", "%3")
     if (DOUBLE) {
-        asm("{\n\t.reg .pred neg, hit;\n\t.reg .b32 lo, hi;\n\t"
-            "setp.ne.u32 hit, %3, %3;\n\t" CTD_S8("%0") "selp.u32 %1, 1, 0, hit;\n\t}"
+        asm(CTD_BLOCK_HEAD CTD_S8("%0") CTD_BLOCK_TAIL("%1")
             : "+l"(u), "=r"(cand)
-            : "l"(p), "r"(tlo), "l"(c));
+            : "l"(p), "r"(ntlo), "l"(c));
     } else {
-        asm("{\n\t.reg .pred neg, hit;\n\t.reg .b32 lo, hi;\n\t"
-            "setp.ne.u32 hit, %3, %3;\n\t" CTD_S8("%4") "selp.u32 %1, 1, 0, hit;\n\t}"
+        asm(CTD_BLOCK_HEAD CTD_S8("%4") CTD_BLOCK_TAIL("%1")
             : "+l"(u), "=r"(cand)
-            : "l"(p), "r"(tlo), "l"(c));
+            : "l"(p), "r"(ntlo), "l"(c));
     }
 #undef CTD_S8
     return cand;
@@ -134,28 +141,36 @@ __device__ __forceinline__ void walk_target(uint64_t u, uint64_t target, uint64_
 }
 
 // walk_target for u <- u + c (DOUBLE: u <- 2u) with p < 2^63, blocks of
-// eight steps in PTX with the candidate predicate kept across the block.
+// eight steps in PTX with 32-bit block counters; a candidate block is
+// replayed from its saved start with the full 64-bit test.
 template <bool DOUBLE>
 __device__ __forceinline__ void walk_add63(uint64_t u, uint64_t c, uint64_t target, uint64_t p, uint64_t idx,
                                            uint64_t steps, const FactorsView &fb)
 {
     if (u == target)
         push(fb, idx, p);
-    const uint32_t tlo = (uint32_t)target;
-    uint64_t i = 0;
-    for (; i + UNROLL <= steps; i += UNROLL) {
-        const uint64_t u0 = u;
-        if (step8_add63<DOUBLE>(u, c, p, tlo)) {
-            uint64_t v = u0;
+    const uint32_t ntlo = 0u - (uint32_t)target;
+    uint64_t nb = steps / UNROLL;
+    uint64_t base = idx;  // index of the state before the current block
+    while (nb) {
+        const uint32_t chunk = nb > 0x40000000ull ? 0x40000000u : (uint32_t)nb;
+        for (uint32_t b = 0; b < chunk; ++b) {
+            const uint64_t u0 = u;
+            if (step8_add63<DOUBLE>(u, c, p, ntlo)) {
+                uint64_t v = u0;
+                const uint64_t at = base + (uint64_t)b * UNROLL;
 #pragma unroll 1
-            for (int j = 0; j < UNROLL; ++j) {
-                v = DOUBLE ? add63(v, v, p) : add63(v, c, p);
-                if (v == target)
-                    push(fb, idx + i + j + 1, p);
+                for (int j = 0; j < UNROLL; ++j) {
+                    v = DOUBLE ? add63(v, v, p) : add63(v, c, p);
+                    if (v == target)
+                        push(fb, at + j + 1, p);
+                }
             }
         }
+        base += (uint64_t)chunk * UNROLL;
+        nb -= chunk;
     }
-    for (; i < steps; ++i) {
+    for (uint64_t i = base - idx; i < steps; ++i) {
         u = DOUBLE ? add63(u, u, p) : add63(u, c, p);
         if (u == target)
             push(fb, idx + i + 1, p);
@@ -261,13 +276,12 @@ __device__ __forceinline__ void run_fibonacci(const JobView &job, uint64_t p, ui
             // a <- a + b, b <- b + a alternately: (a, b) is (S(n-1), S(n))
             // again after every second step, with no register moves
             // operands: %0 = a, %1 = b, %2 = candidate flag, %3 = p, %4 = 0
-            asm("{\n\t.reg .pred neg, hit;\n\t.reg .b32 lo, hi;\n\t"
-                "setp.ne.u32 hit, %4, %4;\n\t"
+            asm(CTD_BLOCK_HEAD
                 CTD_ADD_STEP("%0", "%1", "%3", "%4") CTD_ADD_STEP("%1", "%0", "%3", "%4")
                 CTD_ADD_STEP("%0", "%1", "%3", "%4") CTD_ADD_STEP("%1", "%0", "%3", "%4")
                 CTD_ADD_STEP("%0", "%1", "%3", "%4") CTD_ADD_STEP("%1", "%0", "%3", "%4")
                 CTD_ADD_STEP("%0", "%1", "%3", "%4") CTD_ADD_STEP("%1", "%0", "%3", "%4")
-                "selp.u32 %2, 1, 0, hit;\n\t}"
+                CTD_BLOCK_TAIL("%2")
                 : "+l"(a), "+l"(b), "=r"(cand)
                 : "l"(p), "r"(zero));
             if (cand) {
@@ -334,7 +348,7 @@ __device__ __forceinline__ void trib_triple(const Mont &m, uint64_t n, uint64_t 
     "setp.lt.s64 neg, " X ", 0;\n\t"             \
     "@neg add.u64 " X ", " X ", %4;\n\t"         \
     "mov.b64 {lo, hi}, " X ";\n\t"               \
-    "setp.eq.or.u32 hit, lo, %6, hit;\n\t"
+    "mul.lo.u32 acc, acc, lo;\n\t"
 
 __device__ __forceinline__ uint64_t trib_add(uint64_t x, uint64_t y, uint64_t z, uint64_t p)
 {
@@ -370,12 +384,11 @@ __device__ __forceinline__ void run_tribonacci(const JobView &job, uint64_t p, u
         for (; i + TB <= steps; i += TB) {
             const uint64_t x0 = x, y0 = y, z0 = z;
             uint32_t cand;
-            asm("{\n\t.reg .pred neg, hit;\n\t.reg .b32 lo, hi;\n\t"
-                "setp.ne.u32 hit, %6, %6;\n\t"
+            asm(CTD_BLOCK_HEAD
                 CTD_TRIB_STEP("%0", "%1", "%2") CTD_TRIB_STEP("%1", "%2", "%0")
                 CTD_TRIB_STEP("%2", "%0", "%1") CTD_TRIB_STEP("%0", "%1", "%2")
                 CTD_TRIB_STEP("%1", "%2", "%0") CTD_TRIB_STEP("%2", "%0", "%1")
-                "selp.u32 %3, 1, 0, hit;\n\t}"
+                CTD_BLOCK_TAIL("%3")
                 : "+l"(x), "+l"(y), "+l"(z), "=r"(cand)
                 : "l"(p), "l"(p2), "r"(zero));
             if (cand) {
@@ -570,7 +583,8 @@ __device__ __forceinline__ void run_item(const JobView &job, uint64_t p, uint64_
 }
 
 template <uint32_t FAM>
-__global__ void __launch_bounds__(256) residue_kernel(JobView job, const uint64_t *__restrict__ primes, uint64_t nprimes)
+__global__ void __launch_bounds__(256, (FAM == SMARANDACHE || FAM == TRIBONACCI) ? 4 : 8)
+residue_kernel(JobView job, const uint64_t *__restrict__ primes, uint64_t nprimes)
 {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     const uint64_t first = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
