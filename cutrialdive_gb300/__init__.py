@@ -8,6 +8,7 @@ from ._native import CtdError, CtdJob, load as load_native, lib_path  # noqa: F4
 from .api import (  # noqa: F401
     PEANO,
     Engine,
+    Server,
     dispatch,
     engine,
     factoring_results,

@@ -340,6 +340,66 @@ class Engine:
         self._check(rc, "ctd_run_plain")
 
 
+    def batch_run(self, jobs: list, bufs: list, segment_length: int = 0, use_graph: bool = True) -> None:
+        """ctd_batch_run: several jobs in one chunk-major, graph-captured pass."""
+        n = len(jobs)
+        arr = (N.CtdJob * n)(*jobs)
+        cps = (N.p32 * n)(*[b.counts.ctypes.data_as(N.p32) for b in bufs])
+        fps = (N.p64 * n)(*[b.factors.ctypes.data_as(N.p64) for b in bufs])
+        self._check(self._L.ctd_batch_run(self._h, arr, n, cps, fps, segment_length, 1 if use_graph else 0),
+                    "ctd_batch_run")
+
+
+class Server:
+    """Continuous-batching server over ctd_serve_* (one device context)."""
+
+    def __init__(self, eng: Engine, memory_budget: int = 160 << 30, max_active: int = 256,
+                 segment_length: int = 1 << 30):
+        self._eng = eng
+        self._L = eng._L
+        h = ctypes.c_void_p()
+        eng._check(self._L.ctd_serve_open(eng.handle, memory_budget, max_active, segment_length, ctypes.byref(h)),
+                   "ctd_serve_open")
+        self._h = h
+        self._jobs: dict = {}
+
+    def submit(self, job: N.CtdJob) -> int:
+        jid = ctypes.c_uint64()
+        self._eng._check(self._L.ctd_serve_submit(self._h, ctypes.byref(job), ctypes.byref(jid)), "ctd_serve_submit")
+        self._jobs[jid.value] = job
+        return jid.value
+
+    def tick(self) -> list[int]:
+        cap = max(len(self._jobs), 1)
+        ids = (ctypes.c_uint64 * cap)()
+        nd = ctypes.c_uint32()
+        self._eng._check(self._L.ctd_serve_tick(self._h, ids, cap, ctypes.byref(nd)), "ctd_serve_tick")
+        return [ids[i] for i in range(min(nd.value, cap))]
+
+    def fetch(self, jid: int) -> factors_buffer:
+        job = self._jobs.pop(jid)
+        buf = factors_buffer.empty(job.n0, job.n1 - job.n0, job.max_factors)
+        self._eng._check(self._L.ctd_serve_fetch(self._h, jid, buf.counts.ctypes.data_as(N.p32),
+                                                 buf.factors.ctypes.data_as(N.p64)), "ctd_serve_fetch")
+        return buf
+
+    def status(self) -> dict:
+        a, q, m = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint64()
+        self._L.ctd_serve_status(self._h, ctypes.byref(a), ctypes.byref(q), ctypes.byref(m))
+        return {"active": a.value, "queued": q.value, "memory_used": m.value}
+
+    def close(self) -> None:
+        if self._h:
+            self._L.ctd_serve_close(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 _engines: dict = {}
 
 

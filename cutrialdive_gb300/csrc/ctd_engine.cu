@@ -162,6 +162,7 @@ namespace ctd {
 int ctx_device(const ctd_ctx *ctx) { return ctx->device; }
 int ctx_sm_count(const ctd_ctx *ctx) { return ctx->sm_count; }
 cudaStream_t ctx_stream(const ctd_ctx *ctx) { return ctx->stream; }
+SieveWorkspace *ctx_workspace(const ctd_ctx *ctx) { return ctx->ws; }
 int ctx_fail(ctd_ctx *ctx, int code, const std::string &msg) { return fail(ctx, code, msg); }
 }  // namespace ctd
 

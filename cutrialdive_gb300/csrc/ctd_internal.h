@@ -98,6 +98,34 @@ int sieve_range_scratch(const SieveScratch &sc, int sm_count, uint64_t lo, uint6
 // nprimes x view.tiles work items.
 int launch_residues(const JobView &view, const uint64_t *d_primes, uint64_t nprimes, int grid, int block,
                     cudaStream_t stream, std::string &err);
+// One job of a batched launch: its view (factors buffer, index range) and
+// its prime range [f0, f1).
+struct BatchJob {
+    JobView view;
+    uint64_t f0, f1;
+};
+// Per active job of a batched launch: first prime index of its sub-range,
+// item count, exclusive item prefix (entry nactive holds the total).
+struct BatchSpan {
+    uint64_t pbeg;
+    uint64_t items;
+    uint64_t prefix;
+};
+// Bounds kernel + one batched residue kernel over the active jobs (all of
+// `family`) for the primes of [lo, hi) in d_primes; the prime count is read
+// from *d_count on the device.  d_spans holds nactive + 1 entries.
+int launch_batch(uint32_t family, const BatchJob *d_jobs, const uint32_t *d_active, uint32_t nactive,
+                 const uint64_t *d_primes, const uint64_t *d_count, uint64_t lo, uint64_t hi, BatchSpan *d_spans,
+                 int grid, cudaStream_t stream, std::string &err);
+int batch_blocks_per_sm(uint32_t family);
+// Odd primes of [lo, hi) into d_out without waiting on the host; the count
+// is left at *count_out (device memory, owned by the workspace).  Base primes
+// must already cover sqrt(hi) (sieve_prepare_base).
+int sieve_prepare_base(SieveWorkspace *ws, uint64_t hi, cudaStream_t stream, std::string &err);
+int sieve_prepare_windows(SieveWorkspace *ws, uint64_t max_width, std::string &err);
+int sieve_odd_async(SieveWorkspace *ws, uint64_t lo, uint64_t hi, uint64_t *d_out, uint64_t capacity,
+                    const uint64_t **count_out, cudaStream_t stream, std::string &err);
+
 // Resident CTAs per SM of the family's residue kernel at `block` threads
 // (0 if the query fails); the persistent grid is SMs x this.
 int residue_blocks_per_sm(uint32_t family, int block);
@@ -111,6 +139,7 @@ void note_kernel_launch();
 int ctx_device(const ctd_ctx *ctx);
 int ctx_sm_count(const ctd_ctx *ctx);
 cudaStream_t ctx_stream(const ctd_ctx *ctx);
+SieveWorkspace *ctx_workspace(const ctd_ctx *ctx);
 int ctx_fail(ctd_ctx *ctx, int code, const std::string &msg);
 
 }  // namespace ctd

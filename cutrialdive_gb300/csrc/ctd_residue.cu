@@ -604,6 +604,153 @@ residue_kernel(JobView job, const uint64_t *__restrict__ primes, uint64_t nprime
     }
 }
 
+// ------------------------------------------------------ batched launches
+// Several jobs over one segment's prime list.  A bounds kernel finds each
+// active job's sub-range of the (sorted) primes and the exclusive prefix of
+// their item counts, reading the prime count from device memory so nothing
+// waits on the host; then one launch per family walks every (job, prime)
+// item.  Used by the batched and served engines (ctd_batch.cu).
+
+__device__ __forceinline__ uint64_t lower_bound_u64(const uint64_t *a, uint64_t n, uint64_t x)
+{
+    uint64_t lo = 0, hi = n;
+    while (lo < hi) {
+        uint64_t mid = (lo + hi) >> 1;
+        if (a[mid] < x)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(1024) batch_bounds_kernel(const BatchJob *__restrict__ jobs,
+                                                            const uint32_t *__restrict__ active, uint32_t nactive,
+                                                            const uint64_t *__restrict__ primes,
+                                                            const uint64_t *__restrict__ d_count, uint64_t lo,
+                                                            uint64_t hi, BatchSpan *__restrict__ spans)
+{
+    const uint64_t n = *d_count;
+    for (uint32_t i = threadIdx.x; i < nactive; i += blockDim.x) {
+        const BatchJob &j = jobs[active[i]];
+        const uint64_t a = j.f0 > lo ? j.f0 : lo;
+        const uint64_t b = j.f1 < hi ? j.f1 : hi;
+        uint64_t pb = 0, pe = 0;
+        if (a < b) {
+            pb = lower_bound_u64(primes, n, a);
+            pe = lower_bound_u64(primes, n, b);
+        }
+        spans[i].pbeg = pb;
+        spans[i].items = pe - pb;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint64_t run = 0;
+        for (uint32_t i = 0; i < nactive; ++i) {
+            spans[i].prefix = run;
+            run += spans[i].items;
+        }
+        spans[nactive].prefix = run;  // total items
+    }
+}
+
+template <uint32_t FAM>
+__global__ void __launch_bounds__(256, (FAM == SMARANDACHE || FAM == TRIBONACCI) ? 4 : 8)
+batch_kernel(const BatchJob *__restrict__ jobs, const uint32_t *__restrict__ active, uint32_t nactive,
+             const uint64_t *__restrict__ primes, const BatchSpan *__restrict__ spans)
+{
+    const uint64_t total = spans[nactive].prefix;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += stride) {
+        // the active job holding item k: last prefix <= k
+        uint32_t lo = 0, hi = nactive;
+        while (hi - lo > 1) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (spans[mid].prefix <= k)
+                lo = mid;
+            else
+                hi = mid;
+        }
+        const BatchJob &j = jobs[active[lo]];
+        const uint64_t p = primes[spans[lo].pbeg + (k - spans[lo].prefix)];
+        run_item<FAM>(j.view, p, j.view.n0, j.view.n1);
+    }
+}
+
+template <uint32_t FAM>
+static cudaError_t launch_batch_fam(const BatchJob *jobs, const uint32_t *active, uint32_t nactive,
+                                    const uint64_t *primes, const BatchSpan *spans, int grid, cudaStream_t st)
+{
+    batch_kernel<FAM><<<grid, 256, 0, st>>>(jobs, active, nactive, primes, spans);
+    return cudaGetLastError();
+}
+
+int launch_batch(uint32_t family, const BatchJob *d_jobs, const uint32_t *d_active, uint32_t nactive,
+                 const uint64_t *d_primes, const uint64_t *d_count, uint64_t lo, uint64_t hi, BatchSpan *d_spans,
+                 int grid, cudaStream_t st, std::string &err)
+{
+    if (!nactive)
+        return CTD_OK;
+    batch_bounds_kernel<<<1, 1024, 0, st>>>(d_jobs, d_active, nactive, d_primes, d_count, lo, hi, d_spans);
+    cudaError_t rc = cudaGetLastError();
+    if (rc == cudaSuccess) {
+        note_kernel_launch();
+        switch (family) {
+        case MERSENNE: rc = launch_batch_fam<MERSENNE>(d_jobs, d_active, nactive, d_primes, d_spans, grid, st); break;
+        case PROTH: rc = launch_batch_fam<PROTH>(d_jobs, d_active, nactive, d_primes, d_spans, grid, st); break;
+        case RIESEL: rc = launch_batch_fam<RIESEL>(d_jobs, d_active, nactive, d_primes, d_spans, grid, st); break;
+        case SMARANDACHE:
+            rc = launch_batch_fam<SMARANDACHE>(d_jobs, d_active, nactive, d_primes, d_spans, grid, st);
+            break;
+        case FIBONACCI: rc = launch_batch_fam<FIBONACCI>(d_jobs, d_active, nactive, d_primes, d_spans, grid, st); break;
+        case LUCAS: rc = launch_batch_fam<LUCAS>(d_jobs, d_active, nactive, d_primes, d_spans, grid, st); break;
+        case PROTH_FIXED_N:
+            rc = launch_batch_fam<PROTH_FIXED_N>(d_jobs, d_active, nactive, d_primes, d_spans, grid, st);
+            break;
+        case RIESEL_FIXED_N:
+            rc = launch_batch_fam<RIESEL_FIXED_N>(d_jobs, d_active, nactive, d_primes, d_spans, grid, st);
+            break;
+        case TRIBONACCI:
+            rc = launch_batch_fam<TRIBONACCI>(d_jobs, d_active, nactive, d_primes, d_spans, grid, st);
+            break;
+        case PEANO: rc = launch_batch_fam<PEANO>(d_jobs, d_active, nactive, d_primes, d_spans, grid, st); break;
+        default: err = "unknown sequence family"; return CTD_ERR_INVALID_ARGUMENT;
+        }
+    }
+    if (rc != cudaSuccess) {
+        err = std::string("batched residue launch: ") + cudaGetErrorString(rc);
+        return CTD_ERR_CUDA;
+    }
+    note_kernel_launch();
+    return CTD_OK;
+}
+
+template <uint32_t FAM>
+static int batch_occupancy(int block)
+{
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<FAM>, block, 0) != cudaSuccess)
+        return 0;
+    return n;
+}
+
+int batch_blocks_per_sm(uint32_t family)
+{
+    switch (family) {
+    case MERSENNE: return batch_occupancy<MERSENNE>(256);
+    case PROTH: return batch_occupancy<PROTH>(256);
+    case RIESEL: return batch_occupancy<RIESEL>(256);
+    case SMARANDACHE: return batch_occupancy<SMARANDACHE>(256);
+    case FIBONACCI: return batch_occupancy<FIBONACCI>(256);
+    case LUCAS: return batch_occupancy<LUCAS>(256);
+    case PROTH_FIXED_N: return batch_occupancy<PROTH_FIXED_N>(256);
+    case RIESEL_FIXED_N: return batch_occupancy<RIESEL_FIXED_N>(256);
+    case TRIBONACCI: return batch_occupancy<TRIBONACCI>(256);
+    case PEANO: return batch_occupancy<PEANO>(256);
+    default: return 0;
+    }
+}
+
 // --------------------------------------------------------- the prime 2
 // value_mod_2 / next_value_mod_2 of each family (number_sequence_helpers.hpp:14-37
 // and the per-family closed forms cited in the oracle).

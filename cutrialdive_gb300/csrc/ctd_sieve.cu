@@ -460,6 +460,60 @@ uint64_t prime_count_upper_bound(uint64_t lo, uint64_t hi)
     return (uint64_t)bound + 64;
 }
 
+// ------------------------------------------------ launch-only variant
+// For the batched engine: base primes and window scratch are prepared once,
+// then each segment is three kernel launches with the prime count left in
+// device memory -- no allocation and no host wait, so a whole schedule of
+// segments can be captured in one CUDA graph.
+int sieve_prepare_base(SieveWorkspace *ws, uint64_t hi, cudaStream_t st, std::string &err)
+{
+    if (hi < 3)
+        return CTD_OK;
+    return ensure_base(ws, isqrt64(hi - 1), st, err);
+}
+
+int sieve_prepare_windows(SieveWorkspace *ws, uint64_t max_width, std::string &err)
+{
+    const uint64_t nwin = (max_width / 2 + 1 + WIN_ODD - 1) / WIN_ODD + 1;
+    int rc = ensure_windows(ws, nwin, err);
+    if (rc)
+        return rc;
+    const size_t smem = WIN_WORDS * sizeof(uint32_t);
+    CUDA_TRY(cudaFuncSetAttribute(sieve_windows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    return CTD_OK;
+}
+
+int sieve_odd_async(SieveWorkspace *ws, uint64_t lo, uint64_t hi, uint64_t *d_out, uint64_t capacity,
+                    const uint64_t **count_out, cudaStream_t st, std::string &err)
+{
+    const uint64_t lo_odd = lo < 3 ? 3 : (lo | 1);
+    const uint64_t nodd = lo_odd < hi ? (hi - lo_odd + 1) / 2 : 0;
+    const uint64_t nwin = nodd ? (nodd + WIN_ODD - 1) / WIN_ODD : 0;
+    if (nwin > ws->win_cap || !ws->d_base) {
+        err = "sieve scratch not prepared for this segment";
+        return CTD_ERR_INVALID_ARGUMENT;
+    }
+    *count_out = ws->d_offsets + nwin;
+    if (!nwin) {  // empty: a zero count
+        CUDA_TRY(cudaMemsetAsync(ws->d_offsets, 0, sizeof(uint64_t), st));
+        return CTD_OK;
+    }
+    const size_t smem = WIN_WORDS * sizeof(uint32_t);
+    const int grid = grid_for(ws, nwin);
+    sieve_windows<<<grid, SIEVE_THREADS, smem, st>>>(lo_odd, nodd, (uint32_t)nwin, ws->d_base, ws->nbase, ws->d_bits,
+                                                    ws->d_wcount);
+    CUDA_TRY(cudaGetLastError());
+    scan_counts<<<1, 1024, 0, st>>>(ws->d_wcount, (uint32_t)nwin, ws->d_offsets);
+    CUDA_TRY(cudaGetLastError());
+    compact_windows<uint64_t><<<grid, SIEVE_THREADS, 0, st>>>(lo_odd, (uint32_t)nwin, ws->d_bits, ws->d_offsets,
+                                                              d_out, capacity, 0);
+    CUDA_TRY(cudaGetLastError());
+    note_kernel_launch();
+    note_kernel_launch();
+    note_kernel_launch();
+    return CTD_OK;
+}
+
 // ----------------------------------------------- fixed-scratch variant
 // The same three-pass sieve over scratch the caller provides (no device
 // allocation, no cached state): base primes are recomputed on every call

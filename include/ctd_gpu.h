@@ -151,6 +151,37 @@ int ctd_residues_device(ctd_ctx *ctx, const ctd_job *job, const uint64_t *d_prim
 /* The prime-2 pass into a device factors buffer (src/trial_factoring.cuh:139-154). */
 int ctd_mod2_device(ctd_ctx *ctx, const ctd_job *job, uint32_t *d_counts, uint64_t *d_factors, void *stream);
 
+/* ---- many jobs ----
+ * No counterpart in the reference (one job per process there,
+ * src/main.cpp:94-146); built from the same per-job semantics as
+ * ctd_run_plain, so each job's factors buffer comes out exactly as a
+ * ctd_run_plain of that job alone would leave it (slot order aside). */
+
+/* Runs `njobs` jobs together: the union of their prime ranges is walked in
+ * aligned segments of `segment_length` (0 = 2^30); each segment is sieved
+ * once on the device and consumed by every job covering it with one batched
+ * residue launch per family.  With use_graph != 0 the whole schedule is
+ * captured into one CUDA graph and launched once.  counts_inout[i] /
+ * factors_inout[i] are job i's host factors buffers (resume state in,
+ * results out). */
+int ctd_batch_run(ctd_ctx *ctx, const ctd_job *jobs, uint32_t njobs, uint32_t *const *counts_inout,
+                  uint64_t *const *factors_inout, uint64_t segment_length, int use_graph);
+
+/* Continuous-batching server.  Submitted jobs queue; each ctd_serve_tick
+ * admits queued jobs (arrival order) while fewer than max_active run and
+ * their device buffers fit memory_budget, then advances every active job
+ * over its next aligned prime segment in shared batched launches, and
+ * reports the jobs that finished; ctd_serve_fetch returns (and releases) a
+ * finished job's factors buffer. */
+typedef struct ctd_server ctd_server;
+int ctd_serve_open(ctd_ctx *ctx, uint64_t memory_budget, uint32_t max_active, uint64_t segment_length,
+                   ctd_server **out);
+void ctd_serve_close(ctd_server *srv);
+int ctd_serve_submit(ctd_server *srv, const ctd_job *job, uint64_t *id);
+int ctd_serve_tick(ctd_server *srv, uint64_t *done_ids, uint32_t cap, uint32_t *ndone);
+int ctd_serve_fetch(ctd_server *srv, uint64_t id, uint32_t *counts, uint64_t *factors);
+int ctd_serve_status(ctd_server *srv, uint32_t *active, uint32_t *queued, uint64_t *memory_used);
+
 /* ---- allocation-free device sieve ----
  * No counterpart in the reference.  For callers that may not allocate device
  * memory -- a process that reserves its whole memory budget at start-up and
