@@ -358,6 +358,166 @@ def run_ours(args, world, rank, local):
     return 0
 
 
+# ------------------------------------------------- batched / served workloads
+BATCHED_WORKLOAD = ("Batched: 64 heterogeneous jobs drawn from seed 1234 (families uniform over smarandache b 2..16, "
+                    "riesel k odd in [3, 10^6], proth_fixed_n n in [1000, 20000], mersenne; index ranges log-uniform "
+                    "in [100, 20000] starting in [1, 50000]; TF range [2^a, 2^(a+2)), a in 30..38)")
+
+
+def same_results(a, b) -> bool:
+    """Equal counts, and equal sorted factor lists wherever no term overflowed
+    its slots (which primes an overflowing term keeps depends on arrival order)."""
+    import numpy as np
+
+    if not np.array_equal(a.counts, b.counts):
+        return False
+    m = a.max_factors_per_number
+    ra, rb = a.to_factoring_results(), b.to_factoring_results()
+    return all(ra[i] == rb[i] for i in range(len(ra)) if a.counts[i] <= m)
+
+
+def job_updates(eng, jobs) -> int:
+    """Exact residue updates of a job list: primes in [f0, f1) x terms."""
+    total = 0
+    for j in jobs:
+        total += eng.prime_count(j.f0, j.f1) * (j.n1 - j.n0)
+    return total
+
+
+def run_batched(args, world, rank, local):
+    import torch
+
+    import cutrialdive_gb300 as ctd
+    from cutrialdive_gb300 import _native as NAT
+    from cutrialdive_gb300 import jobs as J
+
+    torch.cuda.set_device(local)
+    if rank != 0:
+        return 0
+    L = NAT.load()
+    eng = ctd.Engine(local)
+    mix = J.batched_mix()
+    jobs = [j.ctd(MAXF, args.shrink) for j in mix]
+    updates = job_updates(eng, jobs)
+
+    def bufs():
+        return [ctd.factors_buffer.empty(j.n0, j.n1 - j.n0, MAXF) for j in jobs]
+
+    def batched_pass():
+        b = bufs()
+        eng.batch_run(jobs, b, segment_length=1 << 30, use_graph=True)
+        return b
+
+    def sequential_pass():
+        b = bufs()
+        for j, x in zip(jobs, b):
+            eng.run_plain(j, x)
+        return b
+
+    for _ in range(args.warmup):
+        out_b = batched_pass()
+    l0 = L.ctd_kernel_launches()
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            out_b = batched_pass()
+        torch.cuda.synchronize()
+        tb = (time.perf_counter() - t0) / args.steps
+    launches = (L.ctd_kernel_launches() - l0) // args.steps
+    out_s = sequential_pass()  # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    seq_steps = max(1, min(args.steps, 2))
+    for _ in range(seq_steps):
+        out_s = sequential_pass()
+    torch.cuda.synchronize()
+    ts = (time.perf_counter() - t0) / seq_steps
+    identical = all(same_results(a, b) for a, b in zip(out_b, out_s))
+    h2d = sum((j.n1 - j.n0) * (4 + 8 * MAXF) for j in jobs)
+    line = {
+        "metric": METRIC, "value": updates / tb, "unit": "updates/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * tb, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded job mix, seed 1234)",
+        "config": {"workload": BATCHED_WORKLOAD,
+                   "sample": f"each job's TF range cut to its first 1/{args.shrink}: [2^a, 2^a + 3*2^a/{args.shrink})",
+                   "step": "one ctd_batch_run over all 64 jobs (aligned 2^30 segments, one CUDA graph)",
+                   "l2": "prime lists of a segment (up to about 400 MB) exceed L2"},
+        "updates_per_step": updates,
+        "sequential": {"value": updates / ts, "ms_per_step": 1e3 * ts, "steps": seq_steps,
+                       "api": "ctd_run_plain per job, default 2^26 segments, same host buffers"},
+        "batched_over_sequential": ts / tb, "identical_outputs": identical,
+        "e2e": {"value": updates / tb, "unit": "updates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
+                "api": "ctd_batch_run with host factors buffers (copies inside the call)"},
+        "clocks": clocks.summary(), "gpu_launches": int(launches),
+    }
+    print(json.dumps(line), flush=True)
+    return 0 if identical else 1
+
+
+def run_served(args, world, rank, local):
+    import numpy as np
+    import torch
+
+    import cutrialdive_gb300 as ctd
+    from cutrialdive_gb300 import _native as NAT
+    from cutrialdive_gb300 import jobs as J
+
+    torch.cuda.set_device(local)
+    if rank != 0:
+        return 0
+    L = NAT.load()
+    eng = ctd.Engine(local)
+    rates = [float(r) for r in args.rates.split(",")]
+    sweep = []
+    l0 = L.ctd_kernel_launches()
+    with ClockSampler(local) as clocks:
+        for rate in rates:
+            mix, arrivals = J.served_mix(rate)
+            count = min(len(mix), max(1, int(rate * args.window)))
+            jobs = [j.ctd(MAXF, args.shrink) for j in mix[:count]]
+            arrivals = arrivals[:count]
+            updates = job_updates(eng, jobs)
+            srv = ctd.Server(eng, memory_budget=160 << 30, max_active=256, segment_length=1 << 30)
+            lat, ids, i = [], {}, 0
+            t0 = time.perf_counter()
+            while len(lat) < count:
+                now = time.perf_counter() - t0
+                while i < count and arrivals[i] <= now:
+                    ids[srv.submit(jobs[i])] = i
+                    i += 1
+                st = srv.status()
+                if st["active"] or st["queued"]:
+                    for jid in srv.tick():
+                        srv.fetch(jid)
+                        lat.append(time.perf_counter() - t0 - arrivals[ids.pop(jid)])
+                elif i < count:
+                    time.sleep(max(0.0, min(arrivals[i] - now, 0.05)))
+            span = time.perf_counter() - t0
+            srv.close()
+            sweep.append({"rate_jobs_s": rate, "jobs": count, "p50_s": float(np.percentile(lat, 50)),
+                          "p99_s": float(np.percentile(lat, 99)), "updates": updates,
+                          "updates_per_s": updates / span, "seconds": span})
+    launches = L.ctd_kernel_launches() - l0
+    best = max(sweep, key=lambda r: r["updates_per_s"])
+    line = {
+        "metric": METRIC + "; p50/p99 job latency", "value": best["updates_per_s"], "unit": "updates/s",
+        "n_gpus": 1, "steps": len(rates), "warmup": 0, "ms_per_step": 1e3 * best["seconds"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic (Poisson arrivals of the seeded job mix, seed 99)",
+        "config": {"workload": "Serving: Poisson arrival stream from the batched distribution (seed 99), "
+                               "admission by a 160 GB HBM budget",
+                   "sample": f"each job's TF range cut to its first 1/{args.shrink}; at each rate the jobs "
+                             f"arriving in the first {args.window:g} s (at most 2000)",
+                   "server": "ctd_serve_* with max_active 256, 2^30 segments per tick"},
+        "sweep": sweep, "clocks": clocks.summary(), "gpu_launches": int(launches),
+        "e2e": {"value": best["updates_per_s"], "unit": "updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0, "api": "ctd_serve_submit/tick/fetch (host buffers)"},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main() -> int:
     global SEG, NSEG
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
@@ -369,6 +529,12 @@ def main() -> int:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--segment-bits", type=int, default=30,
                     help="log2 of the prime-segment width of one step (profiling uses smaller cases)")
+    ap.add_argument("--workload", choices=["proth", "batched", "served"], default="proth",
+                    help="proth: the plain single-job line (default); batched: the 64-job mix through "
+                         "ctd_batch_run against the same jobs one by one; served: the Poisson serving sweep")
+    ap.add_argument("--shrink", type=int, default=256, help="batched/served: keep the first 1/shrink of each TF range")
+    ap.add_argument("--rates", default="1,5,10,25,50", help="served: arrival rates in jobs/s")
+    ap.add_argument("--window", type=float, default=10.0, help="served: seconds of arrivals per rate")
     args = ap.parse_args()
     SEG = 1 << args.segment_bits
     NSEG = (F1 - F0) // SEG
@@ -377,6 +543,10 @@ def main() -> int:
     world, rank, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, world, rank)
+    if args.workload == "batched":
+        return run_batched(args, world, rank, local)
+    if args.workload == "served":
+        return run_served(args, world, rank, local)
     return run_ours(args, world, rank, local)
 
 

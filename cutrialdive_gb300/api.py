@@ -314,6 +314,14 @@ class Engine:
     def set_launch(self, grid_size: int = 0, block_size: int = 0) -> None:
         self._check(self._L.ctd_set_launch(self._h, grid_size, block_size), "set_launch")
 
+    def prime_count(self, lo: int, hi: int) -> int:
+        """Number of primes in [lo, hi) (ctd_sieve with no output array)."""
+        count = ctypes.c_uint64()
+        rc = self._L.ctd_sieve(self._h, lo, hi, None, 0, ctypes.byref(count))
+        if rc not in (0, N.CTD_ERR_CAPACITY):
+            self._check(rc, "ctd_sieve")
+        return count.value
+
     def sieve(self, lo: int, hi: int) -> np.ndarray:
         """Primes in [lo, hi) from the device sieve (ctd_sieve)."""
         count = ctypes.c_uint64()
@@ -338,7 +346,6 @@ class Engine:
         rc = self._L.ctd_run_plain(self._h, ctypes.byref(job), buf.counts.ctypes.data_as(N.p32),
                                    buf.factors.ctypes.data_as(N.p64), resume_after_prime, segment_length, cb, None)
         self._check(rc, "ctd_run_plain")
-
 
     def batch_run(self, jobs: list, bufs: list, segment_length: int = 0, use_graph: bool = True) -> None:
         """ctd_batch_run: several jobs in one chunk-major, graph-captured pass."""

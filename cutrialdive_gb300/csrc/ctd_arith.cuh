@@ -35,6 +35,15 @@ CTD_HD uint32_t mulhi32(uint32_t a, uint32_t b)
 #endif
 }
 
+CTD_HD int clz64(uint64_t x)
+{
+#ifdef __CUDA_ARCH__
+    return __clzll((long long)x);
+#else
+    return x ? __builtin_clzll(x) : 64;
+#endif
+}
+
 // a + b mod p for a, b < p < 2^64 (no overflow assumptions)
 CTD_HD uint64_t addmod(uint64_t a, uint64_t b, uint64_t p)
 {
@@ -73,16 +82,25 @@ struct Mont {
         return (uint64_t)0 - x;
     }
 
-    CTD_HD void init(uint64_t modulus)
+    // Everything but r2: enough for pow2/pow/mul/from and for mul(X, y)
+    // with X in Montgomery form and y plain, which returns a plain X*y/R.
+    CTD_HD void init_lite(uint64_t modulus)
     {
         p = modulus;
         pinv = neg_inverse(p);
         one = ((uint64_t)0 - p) % p;  // 2^64 mod p
-        // R^2 mod p = (R mod p) * 2^64 mod p by 64 modular doublings
-        uint64_t x = one;
-        #pragma unroll 8
-        for (int i = 0; i < 64; ++i)
-            x = dblmod(x, p);
+        r2 = 0;
+    }
+
+    // Full set-up, r2 included (needed by to()).  R^2 = 2^64 * R is the
+    // Montgomery form of 2^64: six Montgomery squarings of the form of 2.
+    CTD_HD void init(uint64_t modulus)
+    {
+        init_lite(modulus);
+        uint64_t x = dblmod(one, p);
+        #pragma unroll
+        for (int i = 0; i < 6; ++i)
+            x = mul(x, x);
         r2 = x;
     }
 
@@ -104,17 +122,26 @@ struct Mont {
         return u;
     }
 
-    CTD_HD uint64_t to(uint64_t x) const { return mul(x % p, r2); }
+    CTD_HD uint64_t to(uint64_t x) const { return mul(x < p ? x : x % p, r2); }
     CTD_HD uint64_t from(uint64_t X) const { return mul(X, 1); }
     CTD_HD uint64_t add(uint64_t a, uint64_t b) const { return addmod(a, b, p); }
     CTD_HD uint64_t sub(uint64_t a, uint64_t b) const { return submod(a, b, p); }
     CTD_HD uint64_t dbl(uint64_t a) const { return dblmod(a, p); }
 
-    // (2^e) in Montgomery form, left-to-right binary powering by doubling
+    // (2^e) in Montgomery form: left-to-right binary powering in which a set
+    // bit costs a modular doubling instead of a multiplication.
     CTD_HD uint64_t pow2(uint64_t e) const
     {
-        uint64_t two = dbl(one);
-        return pow(two, e);
+        if (e == 0)
+            return one;
+        int b = 63 - clz64(e);
+        uint64_t r = dbl(one);
+        while (b-- > 0) {
+            r = mul(r, r);
+            if ((e >> b) & 1)
+                r = dbl(r);
+        }
+        return r;
     }
 
     // base^e in Montgomery form (base in Montgomery form)

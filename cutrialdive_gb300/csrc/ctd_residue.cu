@@ -187,11 +187,16 @@ template <uint32_t FAM>
 __device__ __forceinline__ void run_doubling(const JobView &job, uint64_t p, uint64_t s, uint64_t e)
 {
     Mont m;
-    m.init(p);
-    uint64_t U = m.pow2(s);
-    if (FAM != MERSENNE)
-        U = m.mul(U, m.to(job.param));
-    const uint64_t u = m.from(U);
+    m.init_lite(p);
+    const uint64_t U = m.pow2(s);  // 2^s in Montgomery form
+    uint64_t u;
+    if (FAM == MERSENNE) {
+        u = m.from(U);
+    } else {
+        // Montgomery form times a plain k leaves the plain k*2^s mod p
+        const uint64_t k = job.param < p ? job.param : job.param % p;
+        u = m.mul(U, k);
+    }
     const uint64_t target = (FAM == PROTH) ? p - 1 : 1;
     const uint64_t steps = e - s - 1;
     if (p < (1ull << 63))
@@ -207,10 +212,10 @@ template <uint32_t FAM>
 __device__ __forceinline__ void run_fixed_n(const JobView &job, uint64_t p, uint64_t s, uint64_t e)
 {
     Mont m;
-    m.init(p);
-    const uint64_t C = m.pow2(job.param);
+    m.init_lite(p);
+    const uint64_t C = m.pow2(job.param);  // 2^n in Montgomery form
     const uint64_t c = m.from(C);
-    const uint64_t v = m.from(m.mul(m.to(s), C));
+    const uint64_t v = m.mul(C, s < p ? s : s % p);  // plain s*2^n mod p
     const uint64_t target = (FAM == PROTH_FIXED_N) ? p - 1 : 1;
     const uint64_t steps = e - s - 1;
     if (p < (1ull << 63))

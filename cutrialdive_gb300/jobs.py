@@ -43,10 +43,13 @@ class Job:
     def f1(self) -> int:
         return 1 << (self.a + 2)
 
-    def ctd(self, max_factors: int = 32):
+    def ctd(self, max_factors: int = 32, shrink: int = 1):
+        """The job as a ctd_job; shrink > 1 keeps the first 1/shrink of its
+        prime range, [2^a, 2^a + 3 * 2^a / shrink) (a bounded sample)."""
         from ._native import CtdJob
 
-        return CtdJob(FAMILY_IDS[self.family], max_factors, self.param, self.n0, self.n1, self.f0, self.f1)
+        f1 = self.f0 + (self.f1 - self.f0) // shrink
+        return CtdJob(FAMILY_IDS[self.family], max_factors, self.param, self.n0, self.n1, self.f0, f1)
 
 
 def draw_jobs(seed: int, count: int) -> tuple[list[Job], np.random.Generator]:

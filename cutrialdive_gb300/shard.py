@@ -100,3 +100,67 @@ def gpu_compute(spec, opts, f0: int, f1: int, device: int = 0) -> factors_buffer
     if f1 > f0:
         engine(device).run_plain(make_job(spec, sub), buf)
     return buf
+
+
+# --------------------------------------------------------------- factor files
+def parse_factor_file(text: str) -> dict[int, list[int]]:
+    """'<n> - p1, p2' lines (src/factoring_results.hpp:185-201) -> {n: [p...]}."""
+    out: dict[int, list[int]] = {}
+    for ln in text.splitlines():
+        if not ln.strip():
+            continue
+        head, sep, tail = ln.partition(" - ")
+        if not sep:
+            head, tail = ln.rstrip().rstrip("-").strip(), ""
+        n = int(head)
+        ps = [int(x) for x in tail.replace(",", " ").split()]
+        out.setdefault(n, []).extend(ps)
+    return out
+
+
+def merge_factor_files(texts: list[str]) -> str:
+    """Per-term union of factor files over the same terms, each term's primes
+    ascending, in the reference's line format (a term with no factor keeps
+    its trailing space)."""
+    merged: dict[int, set[int]] = {}
+    for t in texts:
+        for n, ps in parse_factor_file(t).items():
+            merged.setdefault(n, set()).update(ps)
+    return "".join(f"{n} - {', '.join(map(str, sorted(merged[n])))}\n" for n in sorted(merged))
+
+
+def _main(argv=None) -> int:
+    import argparse
+    import sys
+
+    ap = argparse.ArgumentParser(prog="python -m cutrialdive_gb300.shard",
+                                 description="Split a TF range into prime-balanced shards, or merge shard factor files.")
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    sp = sub.add_parser("split", help="print one '--tf-start A --tf-end B' line per shard")
+    sp.add_argument("f0", type=int)
+    sp.add_argument("f1", type=int)
+    sp.add_argument("shards", type=int)
+    sp.add_argument("--align", type=int, default=1 << 20)
+    mp = sub.add_parser("merge", help="merge factor files of the same terms into one")
+    mp.add_argument("files", nargs="+")
+    mp.add_argument("-o", "--output")
+    a = ap.parse_args(argv)
+    if a.cmd == "split":
+        for lo, hi in split_prime_range(a.f0, a.f1, a.shards, a.align):
+            print(f"--tf-start {lo} --tf-end {hi}")
+        return 0
+    texts = []
+    for f in a.files:
+        with open(f) as fh:
+            texts.append(fh.read())
+    out = merge_factor_files(texts)
+    if a.output:
+        with open(a.output, "w") as fh:
+            fh.write(out)
+    else:
+        sys.stdout.write(out)
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(_main())

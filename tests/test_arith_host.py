@@ -1,0 +1,49 @@
+"""The residue kernels' modular arithmetic (ctd_arith.cuh), run on the host
+from the same source and checked against Python integers: Montgomery set-up
+(R mod p, R^2 mod p), 2^e by squaring and doubling, and the mixed
+Montgomery-times-plain product that yields k*2^e mod p."""
+import os
+import random
+import shutil
+import subprocess
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module")
+def checker(tmp_path_factory):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    exe = str(tmp_path_factory.mktemp("arith") / "arith_host_check")
+    subprocess.check_call([nvcc, "-O2", "-std=c++17", "-o", exe, os.path.join(HERE, "arith_host_check.cu")])
+    return exe
+
+
+def cases():
+    rnd = random.Random(5)
+    out = [(3, 0, 1), (3, 1, 2), (5, 64, 7), (2**61 - 1, 100000, 3), (2**64 - 59, 12345, 2**64 - 1),
+           (2**63 + 29, 1, 999999), ((1 << 32) + 15, 99999, 3)]
+    for bits in (8, 20, 31, 32, 33, 40, 50, 62, 63, 64):
+        for _ in range(25):
+            p = rnd.getrandbits(bits) | 1 | (1 << (bits - 1))
+            if p < 3:
+                continue
+            out.append((p, rnd.randrange(0, 1 << rnd.choice((1, 8, 17, 40, 64))), rnd.getrandbits(64)))
+    return out
+
+
+def test_montgomery_setup_and_pow2(checker):
+    cs = cases()
+    inp = "".join(f"{p} {e} {k}\n" for p, e, k in cs)
+    res = subprocess.run([checker], input=inp, capture_output=True, text=True, check=True).stdout.split("\n")
+    R = 1 << 64
+    for (p, e, k), line in zip(cs, res):
+        one, r2, pw, kpw, tok = map(int, line.split())
+        assert one == R % p, (p, e)
+        assert r2 == R * R % p, (p, e)
+        assert pw == pow(2, e, p), (p, e)
+        assert kpw == k * pow(2, e, p) % p, (p, e, k)
+        assert tok == k % p, (p, k)

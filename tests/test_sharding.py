@@ -91,3 +91,23 @@ def test_two_rank_gloo_gather_and_merge():
         assert p.exitcode == 0
     for (fam, param, n0, n1, f0, f1), text in zip(CASES, got):
         assert text == O.trial_factor(fam, param, n0, n1, f0, f1, 64, threads=2).format()
+
+
+def test_factor_file_split_and_merge_cli(tmp_path):
+    """The multi-box story as files: one factor file per shard, merged."""
+    fam, param, n0, n1, f0, f1 = CASES[0]
+    parts = shard.split_prime_range(f0, f1, 3, align=1 << 10)
+    paths = []
+    for k, (a, b) in enumerate(parts):
+        p = tmp_path / f"shard{k}.txt"
+        p.write_text(O.trial_factor(fam, param, n0, n1, a, b, 64, threads=2).format())
+        paths.append(str(p))
+    out = tmp_path / "merged.txt"
+    assert shard._main(["merge", *paths, "-o", str(out)]) == 0
+    assert out.read_text() == O.trial_factor(fam, param, n0, n1, f0, f1, 64, threads=2).format()
+
+
+def test_split_cli_prints_ranges(capsys):
+    assert shard._main(["split", "4294967296", "17179869184", "4"]) == 0
+    lines = capsys.readouterr().out.splitlines()
+    assert len(lines) == 4 and lines[0].startswith("--tf-start 4294967296 ") and lines[-1].endswith(" 17179869184")
