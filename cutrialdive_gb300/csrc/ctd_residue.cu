@@ -59,44 +59,44 @@ __device__ __forceinline__ uint64_t add63(uint64_t a, uint64_t b, uint64_t p)
 
 __device__ __forceinline__ uint64_t dbl63(uint64_t u, uint64_t p) { return add63(u, u, p); }
 
-// One step of u <- u + c (c = u for doubling) with the candidate test on the
-// FMA pipe: acc *= (low word of u) - (low word of the target), so acc becomes
-// 0 when a low word matched (a product of nonzero words reaches 0 mod 2^32
-// only by accumulating 32 factors of two: rare false candidates, never a
-// missed one).  The integer ALU pipe, the kernel's bottleneck, is left with
-// the add pair, the sign test and the predicated add pair.
-#define CTD_ADD_STEP(U, C, P, NT)                \
+// One step of u <- u + c (c = u for doubling) with the candidate test folded
+// into the predicate `hit`: hit |= (low word of u == T).  A block whose low
+// words never matched needs no further test; false candidates come at about
+// 2^-32 per step.  (A test accumulated as a product of low-word differences
+// on the multiply pipe was measured 10x slower: products of 32-bit words hit
+// zero often enough -- about 7e-4 per 8-step block -- that the replays kept
+// warps diverged for the rest of their walks.)
+#define CTD_ADD_STEP(U, C, P, T)                 \
     "add.u64 " U ", " U ", " C ";\n\t"           \
     "sub.u64 " U ", " U ", " P ";\n\t"           \
     "setp.lt.s64 neg, " U ", 0;\n\t"             \
     "@neg add.u64 " U ", " U ", " P ";\n\t"      \
     "mov.b64 {lo, hi}, " U ";\n\t"               \
-    "mad.lo.u32 x, lo, 1, " NT ";\n\t"           \
-    "mul.lo.u32 acc, acc, x;\n\t"
+    "setp.eq.or.u32 hit, lo, " T ", hit;\n\t"
 
-#define CTD_BLOCK_HEAD "{\n\t.reg .pred neg, hit;\n\t.reg .b32 lo, hi, x, acc;\n\tmov.u32 acc, 1;\n\t"
-#define CTD_BLOCK_TAIL(OUT) "setp.eq.u32 hit, acc, 0;\n\tselp.u32 " OUT ", 1, 0, hit;\n\t}"
+// R: any 32-bit register operand (clears `hit` by comparing it with itself)
+#define CTD_BLOCK_HEAD(R) "{\n\t.reg .pred neg, hit;\n\t.reg .b32 lo, hi;\n\tsetp.ne.u32 hit, " R ", " R ";\n\t"
+#define CTD_BLOCK_TAIL(OUT) "selp.u32 " OUT ", 1, 0, hit;\n\t}"
 
 // Eight steps of u <- u + c mod p (c == u: doubling) in one block of PTX;
-// returns nonzero when a low word may have equalled the target's
-// (ntlo = -(low word of the target)).
+// returns nonzero when a low word equalled tlo (the target's low word).
 template <bool DOUBLE>
-__device__ __forceinline__ uint32_t step8_add63(uint64_t &u, uint64_t c, uint64_t p, uint32_t ntlo)
+__device__ __forceinline__ uint32_t step8_add63(uint64_t &u, uint64_t c, uint64_t p, uint32_t tlo)
 {
     uint32_t cand;
-    // operands: %0 = u, %1 = candidate flag, %2 = p, %3 = ntlo, %4 = c
+    // operands: %0 = u, %1 = candidate flag, %2 = p, %3 = tlo, %4 = c
 #define CTD_S8(C)                                                                                   \
     CTD_ADD_STEP("%0", C, "%2", "%3") CTD_ADD_STEP("%0", C, "%2", "%3") CTD_ADD_STEP("%0", C, "%2", "%3") \
     CTD_ADD_STEP("%0", C, "%2", "%3") CTD_ADD_STEP("%0", C, "%2", "%3") CTD_ADD_STEP("%0", C, "%2", "%3") \
     CTD_ADD_STEP("%0", C, "%2", "%3") CTD_ADD_STEP("%0", C, "%2", "%3")
     if (DOUBLE) {
-        asm(CTD_BLOCK_HEAD CTD_S8("%0") CTD_BLOCK_TAIL("%1")
+        asm(CTD_BLOCK_HEAD("%3") CTD_S8("%0") CTD_BLOCK_TAIL("%1")
             : "+l"(u), "=r"(cand)
-            : "l"(p), "r"(ntlo), "l"(c));
+            : "l"(p), "r"(tlo), "l"(c));
     } else {
-        asm(CTD_BLOCK_HEAD CTD_S8("%4") CTD_BLOCK_TAIL("%1")
+        asm(CTD_BLOCK_HEAD("%3") CTD_S8("%4") CTD_BLOCK_TAIL("%1")
             : "+l"(u), "=r"(cand)
-            : "l"(p), "r"(ntlo), "l"(c));
+            : "l"(p), "r"(tlo), "l"(c));
     }
 #undef CTD_S8
     return cand;
@@ -149,14 +149,14 @@ __device__ __forceinline__ void walk_add63(uint64_t u, uint64_t c, uint64_t targ
 {
     if (u == target)
         push(fb, idx, p);
-    const uint32_t ntlo = 0u - (uint32_t)target;
+    const uint32_t tlo = (uint32_t)target;
     uint64_t nb = steps / UNROLL;
     uint64_t base = idx;  // index of the state before the current block
     while (nb) {
         const uint32_t chunk = nb > 0x40000000ull ? 0x40000000u : (uint32_t)nb;
         for (uint32_t b = 0; b < chunk; ++b) {
             const uint64_t u0 = u;
-            if (step8_add63<DOUBLE>(u, c, p, ntlo)) {
+            if (step8_add63<DOUBLE>(u, c, p, tlo)) {
                 uint64_t v = u0;
                 const uint64_t at = base + (uint64_t)b * UNROLL;
 #pragma unroll 1
@@ -281,7 +281,7 @@ __device__ __forceinline__ void run_fibonacci(const JobView &job, uint64_t p, ui
             // a <- a + b, b <- b + a alternately: (a, b) is (S(n-1), S(n))
             // again after every second step, with no register moves
             // operands: %0 = a, %1 = b, %2 = candidate flag, %3 = p, %4 = 0
-            asm(CTD_BLOCK_HEAD
+            asm(CTD_BLOCK_HEAD("%4")
                 CTD_ADD_STEP("%0", "%1", "%3", "%4") CTD_ADD_STEP("%1", "%0", "%3", "%4")
                 CTD_ADD_STEP("%0", "%1", "%3", "%4") CTD_ADD_STEP("%1", "%0", "%3", "%4")
                 CTD_ADD_STEP("%0", "%1", "%3", "%4") CTD_ADD_STEP("%1", "%0", "%3", "%4")
@@ -353,7 +353,7 @@ __device__ __forceinline__ void trib_triple(const Mont &m, uint64_t n, uint64_t 
     "setp.lt.s64 neg, " X ", 0;\n\t"             \
     "@neg add.u64 " X ", " X ", %4;\n\t"         \
     "mov.b64 {lo, hi}, " X ";\n\t"               \
-    "mul.lo.u32 acc, acc, lo;\n\t"
+    "setp.eq.or.u32 hit, lo, %6, hit;\n\t"
 
 __device__ __forceinline__ uint64_t trib_add(uint64_t x, uint64_t y, uint64_t z, uint64_t p)
 {
@@ -389,7 +389,7 @@ __device__ __forceinline__ void run_tribonacci(const JobView &job, uint64_t p, u
         for (; i + TB <= steps; i += TB) {
             const uint64_t x0 = x, y0 = y, z0 = z;
             uint32_t cand;
-            asm(CTD_BLOCK_HEAD
+            asm(CTD_BLOCK_HEAD("%6")
                 CTD_TRIB_STEP("%0", "%1", "%2") CTD_TRIB_STEP("%1", "%2", "%0")
                 CTD_TRIB_STEP("%2", "%0", "%1") CTD_TRIB_STEP("%0", "%1", "%2")
                 CTD_TRIB_STEP("%1", "%2", "%0") CTD_TRIB_STEP("%2", "%0", "%1")
@@ -588,7 +588,7 @@ __device__ __forceinline__ void run_item(const JobView &job, uint64_t p, uint64_
 }
 
 template <uint32_t FAM>
-__global__ void __launch_bounds__(256, (FAM == SMARANDACHE || FAM == TRIBONACCI) ? 4 : 8)
+__global__ void __launch_bounds__(256, (FAM == SMARANDACHE || FAM == TRIBONACCI) ? 4 : 6)
 residue_kernel(JobView job, const uint64_t *__restrict__ primes, uint64_t nprimes)
 {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -660,7 +660,7 @@ __global__ void __launch_bounds__(1024) batch_bounds_kernel(const BatchJob *__re
 }
 
 template <uint32_t FAM>
-__global__ void __launch_bounds__(256, (FAM == SMARANDACHE || FAM == TRIBONACCI) ? 4 : 8)
+__global__ void __launch_bounds__(256, (FAM == SMARANDACHE || FAM == TRIBONACCI) ? 4 : 6)
 batch_kernel(const BatchJob *__restrict__ jobs, const uint32_t *__restrict__ active, uint32_t nactive,
              const uint64_t *__restrict__ primes, const BatchSpan *__restrict__ spans)
 {
