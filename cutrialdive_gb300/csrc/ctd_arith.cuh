@@ -128,6 +128,21 @@ struct Mont {
     CTD_HD uint64_t sub(uint64_t a, uint64_t b) const { return submod(a, b, p); }
     CTD_HD uint64_t dbl(uint64_t a) const { return dblmod(a, p); }
 
+    // floor(2^64 / p): 2^64 = mu p + (R mod p), so mu p = -one mod 2^64 and
+    // mu = -one * p^-1 = one * pinv mod 2^64 (an exact division).
+    CTD_HD uint64_t mu() const { return one * pinv; }
+
+    // Shoup's precomputed quotient floor(w 2^64 / p) for a plain w < p
+    // (needs r2).  w 2^64 = w mu p + w one, so the quotient is
+    // w mu + floor(w one / p), and floor(w one / p) = (w one - (w one mod p)) / p
+    // is again an exact division, by p^-1 mod 2^64; w one mod p = to(w).
+    // Every product wraps mod 2^64; the result is exact because it is < 2^64.
+    CTD_HD uint64_t shoup(uint64_t w) const
+    {
+        const uint64_t r = to(w);
+        return w * mu() + (w * one - r) * ((uint64_t)0 - pinv);
+    }
+
     // (2^e) in Montgomery form: left-to-right binary powering in which a set
     // bit costs a modular doubling instead of a multiplication.
     CTD_HD uint64_t pow2(uint64_t e) const

@@ -444,27 +444,30 @@ __device__ __forceinline__ uint64_t class_end(uint64_t b, uint64_t m, uint64_t &
     return pw;
 }
 
-// X (Montgomery form) -> after the steps m = c0 .. c0+t-1 with multiplier Mm (Montgomery form)
+// X (Montgomery form) -> after the steps m = c0 .. c0+t-1 with multiplier Mm
+// (Montgomery form).  Left-to-right over the bits of t, keeping (M^k, G(k),
+// H(k), k) for the prefix k read so far; k itself is kept in Montgomery form
+// (K) and updated by doubling and adding one, so no conversion is needed.
 __device__ __forceinline__ uint64_t affine_jump(const Mont &m, uint64_t X, uint64_t Mm, uint64_t c0, uint64_t t)
 {
     if (!t)
         return X;
-    uint64_t Mt = m.one, G = 0, H = 0, tc = 0;
+    uint64_t Mt = m.one, G = 0, H = 0, K = 0;
+    bool started = false;
     for (int bit = 63 - __clzll(t); bit >= 0; --bit) {
-        if (tc) {
-            uint64_t tR = m.to(tc);
-            uint64_t H2 = m.add(m.add(m.mul(Mt, H), m.mul(tR, G)), H);
+        if (started) {  // k -> 2k
+            const uint64_t H2 = m.add(m.add(m.mul(Mt, H), m.mul(K, G)), H);
             G = m.mul(G, m.add(m.one, Mt));
             Mt = m.mul(Mt, Mt);
             H = H2;
-            tc <<= 1;
+            K = m.dbl(K);
         }
-        if ((t >> bit) & 1) {
-            uint64_t tR = m.to(tc);
-            H = m.add(m.mul(Mm, H), tR);
+        if ((t >> bit) & 1) {  // k -> k + 1
+            H = m.add(m.mul(Mm, H), K);
             G = m.add(m.mul(Mm, G), m.one);
             Mt = m.mul(Mm, Mt);
-            tc += 1;
+            K = m.add(K, m.one);
+            started = true;
         }
     }
     return m.add(m.add(m.mul(Mt, X), m.mul(m.to(c0), G)), H);
@@ -485,6 +488,45 @@ __device__ __forceinline__ uint64_t smarandache_at(const Mont &m, uint64_t b, ui
             break;
     }
     return X;
+}
+
+// Steps m = mm .. mend-1 of x <- x M + m (x in [1, 3p), M < p, Ms its Shoup
+// quotient); SMALL: M < 2^32.  Returns the final x.
+template <bool SMALL>
+__device__ __forceinline__ uint64_t smarandache_walk64(const JobView &job, uint64_t p, uint64_t x, uint64_t M,
+                                                       uint64_t Ms, uint64_t mm, uint64_t mend, uint32_t plo,
+                                                       uint32_t p2lo)
+{
+    auto step = [&](uint64_t v, uint64_t mv) {
+        const uint64_t q = mulhi64(v, Ms);
+        const uint64_t vm = SMALL ? v * (uint64_t)(uint32_t)M : v * M;
+        return vm + mv - q * p;
+    };
+    while (mm + UNROLL <= mend) {
+        const uint64_t x0 = x;
+        bool cand = false;
+#pragma unroll
+        for (int j = 0; j < UNROLL; ++j) {
+            x = step(x, mm + j);
+            cand |= ((uint32_t)x == plo) | ((uint32_t)x == p2lo);
+        }
+        if (cand) {
+            uint64_t y = x0;
+#pragma unroll 1
+            for (int j = 0; j < UNROLL; ++j) {
+                y = step(y, mm + j);
+                if (y == p || y == 2 * p)
+                    push(job.fb, (mm + j) - job.n0, p);
+            }
+        }
+        mm += UNROLL;
+    }
+    for (; mm < mend; ++mm) {
+        x = step(x, mm);
+        if (x == p || x == 2 * p)
+            push(job.fb, mm - job.n0, p);
+    }
+    return x;
 }
 
 __device__ __forceinline__ void run_smarandache(const JobView &job, uint64_t p, uint64_t s, uint64_t e)
@@ -536,6 +578,26 @@ __device__ __forceinline__ void run_smarandache(const JobView &job, uint64_t p, 
                 if (x == p32 || x == p2)
                     push(job.fb, mm - job.n0, p);
             }
+            mcur = mend;
+        }
+        return;
+    }
+    if (p < (1ull << 62) && e <= p) {
+        // 64-bit Shoup path (every m < p): x kept in [1, 3p) as r + m with
+        // r = x M - q p in [0, 2p), q = mulhi(x, floor(M 2^64 / p)); so
+        // x = 0 mod p <=> x == p or x == 2p.  The unrolled body tests the low
+        // words only; a block with a candidate is replayed with the full test.
+        uint64_t x = m.from(X);
+        const uint32_t plo = (uint32_t)p, p2lo = (uint32_t)(2 * p);
+        while (mcur < e) {
+            uint64_t pw;
+            const uint64_t cend = class_end(b, mcur, pw);
+            const uint64_t mend = cend < e ? cend : e;
+            const uint64_t M = pw < p ? pw : pw % p;
+            if (M >> 32)
+                x = smarandache_walk64<false>(job, p, x, M, m.shoup(M), mcur, mend, plo, p2lo);
+            else
+                x = smarandache_walk64<true>(job, p, x, M, m.shoup(M), mcur, mend, plo, p2lo);
             mcur = mend;
         }
         return;

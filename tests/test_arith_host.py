@@ -1,7 +1,8 @@
 """The residue kernels' modular arithmetic (ctd_arith.cuh), run on the host
 from the same source and checked against Python integers: Montgomery set-up
-(R mod p, R^2 mod p), 2^e by squaring and doubling, and the mixed
-Montgomery-times-plain product that yields k*2^e mod p."""
+(R mod p, R^2 mod p), 2^e by squaring and doubling, the mixed
+Montgomery-times-plain product that yields k*2^e mod p, and the
+division-free floor(2^64/p) and Shoup quotients floor(w 2^64/p)."""
 import os
 import random
 import shutil
@@ -41,9 +42,11 @@ def test_montgomery_setup_and_pow2(checker):
     res = subprocess.run([checker], input=inp, capture_output=True, text=True, check=True).stdout.split("\n")
     R = 1 << 64
     for (p, e, k), line in zip(cs, res):
-        one, r2, pw, kpw, tok = map(int, line.split())
+        one, r2, pw, kpw, tok, mu, sh = map(int, line.split())
         assert one == R % p, (p, e)
         assert r2 == R * R % p, (p, e)
         assert pw == pow(2, e, p), (p, e)
         assert kpw == k * pow(2, e, p) % p, (p, e, k)
         assert tok == k % p, (p, k)
+        assert mu == R // p, p
+        assert sh == (k % p) * R // p, (p, k)
