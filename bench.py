@@ -39,6 +39,11 @@ MAXF = 32
 # recurrence u <- 2u mod p on 64-bit words: 2 (2u - p, add with carry),
 # 1 (sign test), 2 (conditional add of p), 1 (zero test of the residue)
 OPS_PER_UPDATE = 6
+# DRAM bytes per prime of residue_kernel<PROTH> from one ncu capture on
+# [2^32, 2^32 + 2^27): 48,436,480 + 1,024 bytes for 6,047,768 primes; traffic
+# grows with the prime count (each prime is read once), so a full launch's
+# traffic is this figure times its primes
+DRAM_BYTES_PER_PRIME = (48436480 + 1024) / 6047768
 METRIC = "prime*term residue updates/s"
 WORKLOAD = ("Proth k=3: 3*2^n+1 for n=1..100000 by residue doubling, all primes in [2^32, 2^34) from the "
             "device sieve; single job, plain kernel")
@@ -320,7 +325,11 @@ def run_ours(args, world, rank, local):
     roofline = {
         "bound": "int_alu", "kernel": "residue_kernel<PROTH>",
         "achieved": achieved / 1e9, "peak": (peak_int / 1e9) if peak_int else None, "unit": "Gop/s",
-        "frac": (achieved / peak_int) if peak_int else None, "traffic": None,
+        "frac": (achieved / peak_int) if peak_int else None,
+        "traffic": DRAM_BYTES_PER_PRIME * statistics.mean(nprimes),
+        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a 2^27-segment launch, "
+                          "scaled by primes per launch (profiles/residue_kernel_proth_k3_seg2p27_full.md)",
+        "algorithmic_bytes": 8 * statistics.mean(nprimes),
         "ops_per_update": OPS_PER_UPDATE, "launch_ms": statistics.mean(resid_ms),
         "peak_source": "measured now: libctd_probe 32-bit add/xor chains (integer ALU issue rate) on this GPU",
     }

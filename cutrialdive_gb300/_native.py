@@ -36,6 +36,14 @@ class CtdProgress(ctypes.Structure):
     _fields_ = [("segment_end", u64), ("last_prime", u64), ("primes_done", u64), ("elapsed_s", ctypes.c_double)]
 
 
+class CtdTuning(ctypes.Structure):
+    _fields_ = [("block_size", i32), ("ctas_per_sm", i32), ("items_per_thread", u32), ("min_tile", u32),
+                ("segment_log2", u32), ("reserved", u32 * 3)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+
+
 PROGRESS_CB = ctypes.CFUNCTYPE(i32, vp, ctypes.POINTER(CtdProgress), i32)
 
 # every symbol include/ctd_gpu.h declares, with its ctypes signature
@@ -62,6 +70,9 @@ SIGNATURES = {
     "ctd_serve_tick": (i32, [vp, p64, u32, ctypes.POINTER(u32)]),
     "ctd_serve_fetch": (i32, [vp, u64, p32, p64]),
     "ctd_serve_status": (i32, [vp, ctypes.POINTER(u32), ctypes.POINTER(u32), p64]),
+    "ctd_get_tuning": (i32, [vp, u32, ctypes.POINTER(CtdTuning)]),
+    "ctd_set_tuning": (i32, [vp, u32, ctypes.POINTER(CtdTuning)]),
+    "ctd_autotune": (i32, [vp, ctypes.POINTER(CtdJob), ctypes.c_double, ctypes.POINTER(CtdTuning)]),
 }
 
 _lib = None

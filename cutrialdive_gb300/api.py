@@ -347,6 +347,26 @@ class Engine:
                                    buf.factors.ctypes.data_as(N.p64), resume_after_prime, segment_length, cb, None)
         self._check(rc, "ctd_run_plain")
 
+    def get_tuning(self, family: int) -> dict:
+        """Launch/tiling parameters in force for a family (ctd_get_tuning)."""
+        t = N.CtdTuning()
+        self._check(self._L.ctd_get_tuning(self._h, family, ctypes.byref(t)), "ctd_get_tuning")
+        return t.as_dict()
+
+    def set_tuning(self, family: int, tuning: dict | None) -> None:
+        """Sets (or with None resets) a family's parameters (ctd_set_tuning)."""
+        if tuning is None:
+            self._check(self._L.ctd_set_tuning(self._h, family, None), "ctd_set_tuning")
+            return
+        t = N.CtdTuning(**{k: int(v) for k, v in tuning.items()})
+        self._check(self._L.ctd_set_tuning(self._h, family, ctypes.byref(t)), "ctd_set_tuning")
+
+    def autotune(self, job: N.CtdJob, budget_s: float = 2.0) -> dict:
+        """Measures and applies the fastest parameters for the job's family (ctd_autotune)."""
+        t = N.CtdTuning()
+        self._check(self._L.ctd_autotune(self._h, ctypes.byref(job), budget_s, ctypes.byref(t)), "ctd_autotune")
+        return t.as_dict()
+
     def batch_run(self, jobs: list, bufs: list, segment_length: int = 0, use_graph: bool = True) -> None:
         """ctd_batch_run: several jobs in one chunk-major, graph-captured pass."""
         n = len(jobs)

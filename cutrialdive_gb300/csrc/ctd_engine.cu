@@ -33,6 +33,9 @@ struct ctd_ctx {
     size_t counts_cap = 0;
     uint64_t *d_factors = nullptr;
     size_t factors_cap = 0;
+    // per-family launch and tiling parameters (ctd_set_tuning / ctd_autotune)
+    ctd_tuning tuning[10] = {};
+    bool tuned[10] = {};
 };
 
 namespace {
@@ -104,7 +107,38 @@ bool job_ok(const ctd_job *job)
     return true;
 }
 
-int default_block(const ctd_ctx *ctx) { return ctx->block_override > 0 ? ctx->block_override : 256; }
+// slot of a family in the tuning tables (the nine num_seq_id families, then PEANO)
+int tuning_slot(uint32_t family) { return family < 9 ? (int)family : 9; }
+
+constexpr uint32_t DEFAULT_ITEMS_PER_THREAD = 8;
+constexpr uint32_t DEFAULT_MIN_TILE = 4096;
+constexpr uint32_t DEFAULT_SEGMENT_LOG2 = 26;
+
+const ctd_tuning *tuning_of(const ctd_ctx *ctx, uint32_t family)
+{
+    const int k = tuning_slot(family);
+    return ctx->tuned[k] ? &ctx->tuning[k] : nullptr;
+}
+
+int default_block(const ctd_ctx *ctx, uint32_t family)
+{
+    if (ctx->block_override > 0)
+        return ctx->block_override;
+    const ctd_tuning *t = tuning_of(ctx, family);
+    return t && t->block_size > 0 ? t->block_size : 256;
+}
+
+// CTAs of `family` at `block` threads in the persistent grid: the resident
+// maximum, or fewer when the tuning says so
+int grid_for(const ctd_ctx *ctx, uint32_t family, int block, int ctas_per_sm)
+{
+    int per_sm = residue_blocks_per_sm(family, block);
+    if (per_sm < 1)
+        per_sm = 1;
+    if (ctas_per_sm > 0 && ctas_per_sm < per_sm)
+        per_sm = ctas_per_sm;
+    return ctx->sm_count * per_sm;
+}
 
 int default_grid(ctd_ctx *ctx, uint32_t family, int block)
 {
@@ -113,32 +147,43 @@ int default_grid(ctd_ctx *ctx, uint32_t family, int block)
     // persistent grid: exactly the CTAs that are resident at once, so every
     // thread strides over the same number of work items and no CTA waits
     // for a second wave
-    int per_sm = residue_blocks_per_sm(family, block);
-    if (per_sm < 1)
-        per_sm = 1;
-    return ctx->sm_count * per_sm;
+    const ctd_tuning *t = tuning_of(ctx, family);
+    return grid_for(ctx, family, block, t ? t->ctas_per_sm : 0);
 }
 
 // index tiles per prime so that short prime lists still fill the GPU,
 // keeping each tile long enough to amortize its jump
-void choose_tiles(const ctd_ctx *ctx, uint64_t nprimes, uint64_t N, int grid, int block, uint32_t &tiles,
-                  uint64_t &tile_len)
+void tiles_for(uint64_t nprimes, uint64_t N, int grid, int block, uint32_t items_per_thread, uint32_t min_tile,
+               uint32_t &tiles, uint64_t &tile_len)
 {
     tiles = 1;
     tile_len = N;
     const uint64_t threads = (uint64_t)grid * block;
-    const uint64_t want = 8 * threads;
-    if (nprimes >= want || N < 2 * 4096)
+    const uint64_t want = (uint64_t)items_per_thread * threads;
+    if (nprimes >= want || N < 2 * (uint64_t)min_tile)
         return;
     uint64_t t = (want + nprimes - 1) / (nprimes ? nprimes : 1);
-    uint64_t tmax = N / 4096;
+    uint64_t tmax = N / min_tile;
     if (t > tmax)
         t = tmax;
     if (t < 1)
         t = 1;
     tile_len = (N + t - 1) / t;
     tiles = (uint32_t)((N + tile_len - 1) / tile_len);
-    (void)ctx;
+}
+
+void choose_tiles(const ctd_ctx *ctx, uint32_t family, uint64_t nprimes, uint64_t N, int grid, int block,
+                  uint32_t &tiles, uint64_t &tile_len)
+{
+    const ctd_tuning *t = tuning_of(ctx, family);
+    tiles_for(nprimes, N, grid, block, t && t->items_per_thread ? t->items_per_thread : DEFAULT_ITEMS_PER_THREAD,
+              t && t->min_tile ? t->min_tile : DEFAULT_MIN_TILE, tiles, tile_len);
+}
+
+uint64_t default_segment(const ctd_ctx *ctx, uint32_t family)
+{
+    const ctd_tuning *t = tuning_of(ctx, family);
+    return 1ull << (t && t->segment_log2 ? t->segment_log2 : DEFAULT_SEGMENT_LOG2);
 }
 
 JobView make_view(const ctd_job *job, uint32_t *d_counts, uint64_t *d_factors)
@@ -262,6 +307,183 @@ int ctd_set_launch(ctd_ctx *ctx, int grid_size, int block_size)
 
 int ctd_check_job(const ctd_job *job) { return job_ok(job) ? CTD_OK : CTD_ERR_INVALID_ARGUMENT; }
 
+int ctd_get_tuning(ctd_ctx *ctx, uint32_t family, ctd_tuning *out)
+{
+    if (!ctx || !out)
+        return CTD_ERR_INVALID_ARGUMENT;
+    const ctd_tuning *t = tuning_of(ctx, family);
+    if (t) {
+        *out = *t;
+        return CTD_OK;
+    }
+    *out = ctd_tuning{};
+    out->block_size = 256;
+    out->ctas_per_sm = residue_blocks_per_sm(family, 256);
+    out->items_per_thread = DEFAULT_ITEMS_PER_THREAD;
+    out->min_tile = DEFAULT_MIN_TILE;
+    out->segment_log2 = DEFAULT_SEGMENT_LOG2;
+    return CTD_OK;
+}
+
+int ctd_set_tuning(ctd_ctx *ctx, uint32_t family, const ctd_tuning *t)
+{
+    if (!ctx)
+        return CTD_ERR_INVALID_ARGUMENT;
+    const int k = tuning_slot(family);
+    if (!t) {
+        ctx->tuned[k] = false;
+        return CTD_OK;
+    }
+    if (t->block_size < 32 || t->block_size > 256 || (t->block_size % 32) || t->ctas_per_sm < 0 ||
+        t->items_per_thread == 0 || t->min_tile == 0 || (t->segment_log2 && (t->segment_log2 < 20 || t->segment_log2 > 40)))
+        return fail(ctx, CTD_ERR_INVALID_ARGUMENT,
+                    "ctd_set_tuning: block_size 32..256 (multiple of 32), ctas_per_sm >= 0, items_per_thread and "
+                    "min_tile > 0, segment_log2 0 or 20..40");
+    ctx->tuning[k] = *t;
+    ctx->tuned[k] = true;
+    return CTD_OK;
+}
+
+int ctd_autotune(ctd_ctx *ctx, const ctd_job *job, double budget_s, ctd_tuning *best)
+{
+    if (!ctx || !best || !job_ok(job) || job->f1 <= job->f0 || !(budget_s > 0))
+        return fail(ctx, CTD_ERR_INVALID_ARGUMENT, "ctd_autotune: bad arguments");
+    CTX_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const auto t0 = std::chrono::steady_clock::now();
+    auto elapsed = [&] { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); };
+    ctd_tuning cur{};
+    ctd_get_tuning(ctx, job->family, &cur);
+    // sample: the job's first prime segment (odd primes only)
+    const uint64_t fx = job->f0 < 3 ? 3 : job->f0;
+    const uint64_t seg = 1ull << (cur.segment_log2 ? cur.segment_log2 : DEFAULT_SEGMENT_LOG2);
+    const uint64_t fy = job->f1 - fx > seg ? fx + seg : job->f1;
+    if (fx >= fy) {
+        *best = cur;
+        return CTD_OK;
+    }
+    const uint64_t N = job->n1 - job->n0;
+    int rc = ensure_buffer(ctx, ctx->d_primes, ctx->primes_cap, prime_count_upper_bound(fx, fy));
+    if (!rc)
+        rc = ensure_buffer(ctx, ctx->d_counts, ctx->counts_cap, N);
+    if (!rc)
+        rc = ensure_buffer(ctx, ctx->d_factors, ctx->factors_cap, N * job->max_factors);
+    if (rc)
+        return rc;
+    std::string err;
+    uint64_t np = 0;
+    rc = sieve_range(ctx->ws, fx, fy, ctx->d_primes, ctx->primes_cap, &np, st, err);
+    if (rc)
+        return fail(ctx, rc, err);
+    if (!np) {
+        *best = cur;
+        return CTD_OK;
+    }
+    cudaEvent_t ea, eb;
+    CTX_CUDA(cudaEventCreate(&ea));
+    CTX_CUDA(cudaEventCreate(&eb));
+    JobView view = make_view(job, ctx->d_counts, ctx->d_factors);
+    // milliseconds of one residue launch over `n` sample primes (best of two
+    // after a warm-up); the counts are cleared so no term overflows
+    auto time_config = [&](const ctd_tuning &c, uint64_t n, float &ms) -> int {
+        const int grid = grid_for(ctx, job->family, c.block_size, c.ctas_per_sm);
+        tiles_for(n, N, grid, c.block_size, c.items_per_thread, c.min_tile, view.tiles, view.tile_len);
+        ms = 1e30f;
+        for (int r = 0; r < 3; ++r) {
+            if (cudaMemsetAsync(ctx->d_counts, 0, N * sizeof(uint32_t), st) != cudaSuccess)
+                return CTD_ERR_CUDA;
+            cudaEventRecord(ea, st);
+            int e = launch_residues(view, ctx->d_primes, n, grid, c.block_size, st, err);
+            if (e)
+                return e;
+            cudaEventRecord(eb, st);
+            if (cudaEventSynchronize(eb) != cudaSuccess)
+                return CTD_ERR_CUDA;
+            float t = 0;
+            cudaEventElapsedTime(&t, ea, eb);
+            if (r && t < ms)
+                ms = t;
+        }
+        return CTD_OK;
+    };
+    ctd_tuning base = cur;
+    base.block_size = 256;
+    base.ctas_per_sm = 0;
+    float best_ms = 0;
+    rc = time_config(base, np, best_ms);
+    // keep one trial near a sixth of the budget: a prefix of the sample primes
+    if (!rc && best_ms * 1e-3 * 3 > budget_s / 6) {
+        const double f = (budget_s / 6) / (best_ms * 1e-3 * 3);
+        const uint64_t floor_n = (uint64_t)ctx->sm_count * 256 * 8;
+        uint64_t n2 = (uint64_t)(np * f);
+        np = n2 > floor_n ? n2 : (floor_n < np ? floor_n : np);
+        rc = time_config(base, np, best_ms);
+    }
+    ctd_tuning winner = base;
+    // launch shape: block size and resident CTAs per SM
+    const int blocks[] = {256, 128, 64};
+    for (int bi = 0; !rc && bi < 3 && elapsed() < budget_s; ++bi) {
+        const int occ = residue_blocks_per_sm(job->family, blocks[bi]);
+        const int cands[] = {occ, occ - 1, occ / 2, (occ * 3) / 4};
+        for (int ci = 0; !rc && ci < 4 && elapsed() < budget_s; ++ci) {
+            const int c = cands[ci];
+            if (c < 1 || (blocks[bi] == 256 && c == occ))
+                continue;
+            ctd_tuning t = base;
+            t.block_size = blocks[bi];
+            t.ctas_per_sm = c;
+            float ms = 0;
+            rc = time_config(t, np, ms);
+            if (!rc && ms < best_ms) {
+                best_ms = ms;
+                winner = t;
+            }
+        }
+    }
+    // tiling: only where it changes the split of this sample
+    const uint32_t items[] = {2, 4, 8, 16, 32};
+    const uint32_t tiles_min[] = {1024, 2048, 4096, 8192, 16384};
+    const int wgrid = grid_for(ctx, job->family, winner.block_size, winner.ctas_per_sm);
+    uint32_t seen_tiles[32];
+    int nseen = 0;
+    {
+        uint32_t tt;
+        uint64_t tl;
+        tiles_for(np, N, wgrid, winner.block_size, winner.items_per_thread, winner.min_tile, tt, tl);
+        seen_tiles[nseen++] = tt;
+    }
+    for (int i = 0; !rc && i < 5 && elapsed() < budget_s; ++i)
+        for (int j = 0; !rc && j < 5 && elapsed() < budget_s; ++j) {
+            ctd_tuning t = winner;
+            t.items_per_thread = items[i];
+            t.min_tile = tiles_min[j];
+            uint32_t tt;
+            uint64_t tl;
+            tiles_for(np, N, wgrid, t.block_size, t.items_per_thread, t.min_tile, tt, tl);
+            bool dup = false;
+            for (int k = 0; k < nseen; ++k)
+                dup |= seen_tiles[k] == tt;
+            if (dup || nseen >= 32)
+                continue;
+            seen_tiles[nseen++] = tt;
+            float ms = 0;
+            rc = time_config(t, np, ms);
+            if (!rc && ms < best_ms) {
+                best_ms = ms;
+                winner = t;
+            }
+        }
+    cudaEventDestroy(ea);
+    cudaEventDestroy(eb);
+    if (rc)
+        return fail(ctx, rc, err.empty() ? std::string("ctd_autotune: CUDA error") : err);
+    const int k = tuning_slot(job->family);
+    ctx->tuning[k] = winner;
+    ctx->tuned[k] = true;
+    *best = winner;
+    return CTD_OK;
+}
+
 int ctd_sieve_device(ctd_ctx *ctx, uint64_t lo, uint64_t hi, uint64_t *d_out, uint64_t capacity, uint64_t *count,
                      void *stream)
 {
@@ -309,9 +531,9 @@ int ctd_residues_device(ctd_ctx *ctx, const ctd_job *job, const uint64_t *d_prim
     CTX_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
     JobView v = make_view(job, d_counts, d_factors);
-    const int block = default_block(ctx);
+    const int block = default_block(ctx, job->family);
     const int grid = default_grid(ctx, job->family, block);
-    choose_tiles(ctx, nprimes, job->n1 - job->n0, grid, block, v.tiles, v.tile_len);
+    choose_tiles(ctx, job->family, nprimes, job->n1 - job->n0, grid, block, v.tiles, v.tile_len);
     std::string err;
     int rc = launch_residues(v, d_primes, nprimes, grid, block, st, err);
     return rc ? fail(ctx, rc, err) : CTD_OK;
@@ -363,8 +585,8 @@ int ctd_run_plain(ctd_ctx *ctx, const ctd_job *job, uint32_t *counts_inout, uint
         if (rc)
             return fail(ctx, rc, err);
     }
-    const uint64_t seg = segment_length ? segment_length : (1ull << 26);
-    const int block = default_block(ctx);
+    const uint64_t seg = segment_length ? segment_length : default_segment(ctx, job->family);
+    const int block = default_block(ctx, job->family);
     const int grid = default_grid(ctx, job->family, block);
     uint64_t last_prime = resume_after_prime;
     uint64_t primes_done = 0;
@@ -381,7 +603,7 @@ int ctd_run_plain(ctd_ctx *ctx, const ctd_job *job, uint32_t *counts_inout, uint
         if (np > ctx->primes_cap)
             return fail(ctx, CTD_ERR_CAPACITY, "prime count above its bound");
         if (np) {
-            choose_tiles(ctx, np, N, grid, block, view.tiles, view.tile_len);
+            choose_tiles(ctx, job->family, np, N, grid, block, view.tiles, view.tile_len);
             rc = launch_residues(view, ctx->d_primes, np, grid, block, st, err);
             if (rc)
                 return fail(ctx, rc, err);

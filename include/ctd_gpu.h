@@ -102,6 +102,29 @@ int ctd_device_info(ctd_ctx *ctx, char *name, size_t name_len, uint64_t *total_m
  * src/trial_factoring.cuh:280-286); 0 restores the default. */
 int ctd_set_launch(ctd_ctx *ctx, int grid_size, int block_size);
 
+/* Launch and tiling parameters of one family's residue kernel (the
+ * reference derives grid and block from occupancy queries and picks a
+ * divisor batch size by segment end, src/trial_factoring.cuh:275-331,472-481;
+ * here they are measured per family by ctd_autotune). */
+typedef struct ctd_tuning {
+    int32_t block_size;        /* threads per CTA: 32..256, a multiple of 32 */
+    int32_t ctas_per_sm;       /* CTAs per SM of the persistent grid; 0 = as many as fit */
+    uint32_t items_per_thread; /* below this many (prime, tile) items per resident thread, index ranges are tiled */
+    uint32_t min_tile;         /* shortest index tile (each tile starts with an O(log n) jump) */
+    uint32_t segment_log2;     /* default prime-segment width of ctd_run_plain, log2; 0 = 26 */
+    uint32_t reserved[3];
+} ctd_tuning;
+
+/* The parameters in force for `family` (defaults until tuned or set). */
+int ctd_get_tuning(ctd_ctx *ctx, uint32_t family, ctd_tuning *out);
+/* Sets them; NULL restores the defaults.  ctd_set_launch overrides still win. */
+int ctd_set_tuning(ctd_ctx *ctx, uint32_t family, const ctd_tuning *t);
+/* Autotuner: times candidate launch shapes and tilings of the job's family on
+ * the job's own first prime segment (its index range, a sample of its primes)
+ * for about `budget_s` seconds, applies the fastest to the context and returns
+ * it in *best.  Results never depend on the tuning, only the speed. */
+int ctd_autotune(ctd_ctx *ctx, const ctd_job *job, double budget_s, ctd_tuning *best);
+
 /* Validates a job like the reference's dispatch and range checks
  * (src/num_seq_dispatch.hpp:120-170, src/trial_factoring_impl.hpp:380-387):
  * CTD_OK, or CTD_ERR_INVALID_ARGUMENT. */

@@ -1,0 +1,47 @@
+"""Autotuner (ctd_autotune / ctd_set_tuning): the chosen launch shape and
+tiling change only the speed; results stay equal to the oracle's."""
+import pytest
+
+import cutrialdive_gb300 as ctd
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def run(eng, job):
+    buf = ctd.factors_buffer.empty(job.n0, job.n1 - job.n0, job.max_factors)
+    eng.run_plain(job, buf)
+    return str(buf.to_factoring_results())
+
+
+@pytest.mark.parametrize("case", [
+    (O.PROTH, 3, 1, 20001, 1 << 32, (1 << 32) + (1 << 22)),
+    (O.SMARANDACHE, 10, 500, 2500, 1 << 30, (1 << 30) + (1 << 22)),
+    (O.TRIBONACCI, 0, 2, 6002, 1 << 20, 1 << 22),
+])
+def test_autotune_keeps_results(eng, case):
+    fam, param, n0, n1, f0, f1 = case
+    job = ctd.CtdJob(fam, 32, param, n0, n1, f0, f1)
+    want = O.trial_factor(fam, param, n0, n1, f0, f1, 32).format()
+    try:
+        best = eng.autotune(job, budget_s=1.0)
+        assert 32 <= best["block_size"] <= 256 and best["block_size"] % 32 == 0
+        assert best["ctas_per_sm"] >= 0 and best["items_per_thread"] > 0 and best["min_tile"] > 0
+        assert eng.get_tuning(fam) == best
+        assert run(eng, job) == want
+        # an extreme but valid shape: still the same factors
+        eng.set_tuning(fam, {"block_size": 64, "ctas_per_sm": 1, "items_per_thread": 32, "min_tile": 1024,
+                             "segment_log2": 22})
+        assert run(eng, job) == want
+    finally:
+        eng.set_tuning(fam, None)
+    assert eng.get_tuning(fam)["segment_log2"] == 26
+
+
+def test_set_tuning_rejects_bad_values(eng):
+    for bad in ({"block_size": 48}, {"block_size": 512}, {"items_per_thread": 0}, {"segment_log2": 50}):
+        t = {"block_size": 256, "ctas_per_sm": 0, "items_per_thread": 8, "min_tile": 4096, "segment_log2": 0}
+        t.update(bad)
+        with pytest.raises(ctd.CtdError):
+            eng.set_tuning(O.PROTH, t)
+    assert eng.get_tuning(O.PROTH)["block_size"] == 256
