@@ -177,6 +177,58 @@ __device__ __forceinline__ void walk_add63(uint64_t u, uint64_t c, uint64_t targ
     }
 }
 
+// ------------------------------------------- baby-step / giant-step walks
+// For the recurrences whose step is an affine map of a single residue --
+// u -> 2u (Proth, Riesel, Mersenne) and v -> v + c (the fixed-n pair) -- the
+// test of BS consecutive terms needs no stepping: term idx + j is a zero of
+// S iff the state at idx equals a per-prime "baby-step target" T_j (the
+// target pulled back j steps: target * 2^-j, or target - j c).  A block of
+// BS terms is then BS compares of the state's low word against the targets'
+// low words, held in registers, and one giant step to the state BS terms on
+// (a Montgomery multiplication by 2^BS, or one modular add of BS c).  The
+// integer ALU, which bounds the per-step walk, does one compare per term
+// instead of a modular add and a compare; the giant step's multiplication
+// runs on the multiply pipe.  A block whose low words matched is replayed
+// term by term with the full test, so results are those of the walk.
+constexpr int BS = 32;
+
+// halving mod odd p < 2^63: x/2 or (x + p)/2
+__device__ __forceinline__ uint64_t half63(uint64_t x, uint64_t p) { return (x + ((x & 1) ? p : 0)) >> 1; }
+
+// Tests the terms idx .. idx + nblk*BS - 1 of u -> 2u (DOUBLE) or
+// u -> u + c, starting from state u at idx; returns the state at
+// idx + nblk*BS.  tlo[j] = low word of the j-step target; W = the giant step
+// (Montgomery form of 2^BS for doubling, BS*c mod p for the add).
+template <bool DOUBLE>
+__device__ __forceinline__ uint64_t bsgs_blocks(const Mont &m, uint64_t u, uint64_t c, uint64_t target,
+                                                const uint32_t (&tlo)[BS], uint64_t W, uint64_t idx,
+                                                uint64_t nblk, const FactorsView &fb)
+{
+    const uint64_t p = m.p;
+    for (uint64_t b = 0; b < nblk; ++b) {
+        const uint32_t lo = (uint32_t)u;
+        bool c0 = false, c1 = false, c2 = false, c3 = false;
+#pragma unroll
+        for (int j = 0; j < BS; j += 4) {
+            c0 |= lo == tlo[j];
+            c1 |= lo == tlo[j + 1];
+            c2 |= lo == tlo[j + 2];
+            c3 |= lo == tlo[j + 3];
+        }
+        if (c0 | c1 | c2 | c3) {
+            uint64_t v = u;
+#pragma unroll 1
+            for (int j = 0; j < BS; ++j) {
+                if (v == target)
+                    push(fb, idx + b * BS + j, p);
+                v = DOUBLE ? add63(v, v, p) : add63(v, c, p);
+            }
+        }
+        u = DOUBLE ? m.mul(u, W) : add63(u, W, p);
+    }
+    return u;
+}
+
 // ------------------------------------------------------------- families
 
 // Proth k*2^n+1, Riesel k*2^n-1, Mersenne 2^n-1 (riesel_proth.hpp:90-115,
@@ -199,7 +251,20 @@ __device__ __forceinline__ void run_doubling(const JobView &job, uint64_t p, uin
     }
     const uint64_t target = (FAM == PROTH) ? p - 1 : 1;
     const uint64_t steps = e - s - 1;
-    if (p < (1ull << 63))
+    const uint64_t nblk = (e - s) / BS;
+    if (p < (1ull << 63) && nblk >= 2) {
+        uint32_t tlo[BS];
+        uint64_t t = target;
+#pragma unroll
+        for (int j = 0; j < BS; ++j) {
+            tlo[j] = (uint32_t)t;
+            t = half63(t, p);
+        }
+        const uint64_t ub = bsgs_blocks<true>(m, u, 0, target, tlo, m.pow2(BS), s - job.n0, nblk, job.fb);
+        const uint64_t done = nblk * BS;  // terms s .. s+done-1 tested
+        if (done < e - s)
+            walk_add63<true>(ub, 0, target, p, s + done - job.n0, e - s - done - 1, job.fb);
+    } else if (p < (1ull << 63))
         walk_add63<true>(u, 0, target, p, s - job.n0, steps, job.fb);
     else
         walk_target(u, target, p, s - job.n0, steps, job.fb, [p](uint64_t x) { return dblmod(x, p); });
@@ -218,7 +283,24 @@ __device__ __forceinline__ void run_fixed_n(const JobView &job, uint64_t p, uint
     const uint64_t v = m.mul(C, s < p ? s : s % p);  // plain s*2^n mod p
     const uint64_t target = (FAM == PROTH_FIXED_N) ? p - 1 : 1;
     const uint64_t steps = e - s - 1;
-    if (p < (1ull << 63))
+    const uint64_t nblk = (e - s) / BS;
+    if (p < (1ull << 63) && nblk >= 2) {
+        uint32_t tlo[BS];
+        uint64_t t = target, W = c;
+        const uint64_t nc = p - c == p ? 0 : p - c;  // -c mod p
+#pragma unroll
+        for (int j = 0; j < BS; ++j) {
+            tlo[j] = (uint32_t)t;
+            t = addmod(t, nc, p);
+        }
+#pragma unroll
+        for (int j = 0; j < 5; ++j)  // BS c = 2^5 c
+            W = dblmod(W, p);
+        const uint64_t vb = bsgs_blocks<false>(m, v, c, target, tlo, W, s - job.n0, nblk, job.fb);
+        const uint64_t done = nblk * BS;
+        if (done < e - s)
+            walk_add63<false>(vb, c, target, p, s + done - job.n0, e - s - done - 1, job.fb);
+    } else if (p < (1ull << 63))
         walk_add63<false>(v, c, target, p, s - job.n0, steps, job.fb);
     else
         walk_target(v, target, p, s - job.n0, steps, job.fb, [p, c](uint64_t x) { return addmod(x, c, p); });
@@ -632,6 +714,14 @@ __device__ __forceinline__ void run_peano(const JobView &job, uint64_t p, uint64
     }
 }
 
+// Resident CTAs of 256 threads the register budget is sized for: the
+// baby-step families keep 32 targets in registers, Smarandache and
+// tribonacci carry wider state.
+constexpr int min_ctas_per_sm(uint32_t fam)
+{
+    return (fam == FIBONACCI || fam == LUCAS || fam == PEANO) ? 6 : 4;
+}
+
 template <uint32_t FAM>
 __device__ __forceinline__ void run_item(const JobView &job, uint64_t p, uint64_t s, uint64_t e)
 {
@@ -650,7 +740,7 @@ __device__ __forceinline__ void run_item(const JobView &job, uint64_t p, uint64_
 }
 
 template <uint32_t FAM>
-__global__ void __launch_bounds__(256, (FAM == SMARANDACHE || FAM == TRIBONACCI) ? 4 : 6)
+__global__ void __launch_bounds__(256, min_ctas_per_sm(FAM))
 residue_kernel(JobView job, const uint64_t *__restrict__ primes, uint64_t nprimes)
 {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -722,7 +812,7 @@ __global__ void __launch_bounds__(1024) batch_bounds_kernel(const BatchJob *__re
 }
 
 template <uint32_t FAM>
-__global__ void __launch_bounds__(256, (FAM == SMARANDACHE || FAM == TRIBONACCI) ? 4 : 6)
+__global__ void __launch_bounds__(256, min_ctas_per_sm(FAM))
 batch_kernel(const BatchJob *__restrict__ jobs, const uint32_t *__restrict__ active, uint32_t nactive,
              const uint64_t *__restrict__ primes, const BatchSpan *__restrict__ spans)
 {
