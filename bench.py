@@ -1,14 +1,21 @@
 #!/usr/bin/env python3
 """Benchmark of the trial-factoring hot path on GB300.
 
-Workload (the metric's plain single-job configuration): Proth k=3,
+Default workload (the metric's plain single-job configuration): Proth k=3,
 S(n) = 3*2^n + 1 for n = 1..100000, trial-factored by every prime in
 [2^32, 2^34) produced by the device sieve.  One step = one 2^30-wide prime
-segment: device sieve -> primes in HBM -> residue kernel; the 12 segments of
-[2^32, 2^34) are the steps (the default --steps 12 covers the range once).
-Unit of work: one (n, p) residue update; value = updates / s.
+segment: device sieve -> primes in HBM -> residue kernel; the default 12
+steps cover the range once.  Unit of work: one (n, p) residue update;
+value = updates / s.
 
-  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+Other workloads (--workload): `linear` (Fibonacci, Lucas and tribonacci,
+n = 1..50000, primes in [2^34, 2^36), one 2^30 segment of all three jobs per
+step), `smarandache` (base 10, n = 10..1000, all primes below 2^28, the whole
+configuration per step), `batched` (the 64-job mix through ctd_batch_run,
+against the same jobs one by one through ctd_run_plain) and `served` (Poisson
+arrivals through the ctd_serve_* server, p50/p99 latency per rate).
+
+  python bench.py [--gpus N --steps K --warmup W] [--workload W] [--impl reference]
 
 Prints one JSON line (rank 0).  `--impl reference` times the reference
 algorithm on the host cores instead (the CPU oracle, a restatement of the
@@ -30,23 +37,64 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-FAMILY, PARAM, N0, N1 = 1, 3, 1, 100001          # proth, k = 3, n in [1, 100001)
-F0, F1 = 1 << 32, 1 << 34
-SEG = 1 << 30
-NSEG = (F1 - F0) // SEG
 MAXF = 32
-# algorithmic 32-bit integer operations per update of the doubling
-# recurrence u <- 2u mod p on 64-bit words: 2 (2u - p, add with carry),
-# 1 (sign test), 2 (conditional add of p), 1 (zero test of the residue)
-OPS_PER_UPDATE = 6
-# DRAM bytes per prime of residue_kernel<PROTH> from one ncu capture on
-# [2^32, 2^32 + 2^27): 48,436,480 + 1,024 bytes for 6,047,768 primes; traffic
-# grows with the prime count (each prime is read once), so a full launch's
-# traffic is this figure times its primes
-DRAM_BYTES_PER_PRIME = (48436480 + 1024) / 6047768
 METRIC = "prime*term residue updates/s"
-WORKLOAD = ("Proth k=3: 3*2^n+1 for n=1..100000 by residue doubling, all primes in [2^32, 2^34) from the "
-            "device sieve; single job, plain kernel")
+
+
+class Plain:
+    """A plain-kernel workload: jobs (family, param, n0, n1) trial-factored
+    by every prime of [f0, f1), walked in segments of 2^seg_bits; one step =
+    one segment for every job (device sieve once, one residue launch per job)."""
+
+    def __init__(self, name, jobs, f0, f1, seg_bits, text, steps):
+        self.name, self.jobs, self.f0, self.f1, self.seg_bits = name, jobs, f0, f1, seg_bits
+        self.text, self.default_steps = text, steps
+
+    @property
+    def seg(self) -> int:
+        return 1 << self.seg_bits
+
+    @property
+    def nseg(self) -> int:
+        return max(1, -(-(self.f1 - self.f0) // self.seg))
+
+    def segment(self, j: int) -> tuple[int, int]:
+        fx = self.f0 + (j % self.nseg) * self.seg
+        return fx, min(fx + self.seg, self.f1)
+
+
+PLAIN = {
+    "proth": Plain("proth", [(1, 3, 1, 100001)], 1 << 32, 1 << 34, 30,
+                   "Proth k=3: 3*2^n+1 for n=1..100000, all primes in [2^32, 2^34) from the device sieve; "
+                   "single job, plain kernel", 12),
+    "linear": Plain("linear", [(4, 0, 1, 50001), (5, 0, 1, 50001), (8, 0, 1, 50001)], 1 << 34, 1 << 36, 30,
+                    "Linear recurrences: Fibonacci, Lucas and tribonacci for n=1..50000, primes in [2^34, 2^36); "
+                    "three jobs back to back through the plain kernel", 3),
+    "smarandache": Plain("smarandache", [(3, 10, 10, 1001)], 2, 1 << 28, 28,
+                         "Plain Smarandache base 10, Sm(n) for n=10..1000, trial-factored by all primes in "
+                         "[2, 2^28)", 12),
+}
+FAMILY_NAMES = {0: "MERSENNE", 1: "PROTH", 2: "RIESEL", 3: "SMARANDACHE", 4: "FIBONACCI", 5: "LUCAS",
+                6: "PROTH_FIXED_N", 7: "RIESEL_FIXED_N", 8: "TRIBONACCI"}
+# Algorithmic integer-ALU operations per update, by family (32-bit ops of the
+# exact algorithm the kernel runs; multiplies, which go to the multiply pipe,
+# are listed separately):
+#  * doubling (Proth/Riesel/Mersenne) and fixed-n: baby-step/giant-step
+#    blocks of 32 terms: 32 low-word compares + the giant step's adds and
+#    compares (8 for a Montgomery multiplication, 5 for a modular add) per
+#    block -> 40/32 and 37/32;
+#  * Fibonacci/Lucas: modular add (2 add, 1 sign test, 2 predicated add) +
+#    1 compare = 6;
+#  * tribonacci: two-term add and -2p (4), two sign tests and predicated
+#    adds (6), compare (1) = 11;
+#  * Smarandache (64-bit Shoup): adds/subtracts of x M + m - q p (4) and
+#    two low-word compares = 6, plus 9 32-bit multiplies.
+ALU_OPS_PER_UPDATE = {0: 40 / 32, 1: 40 / 32, 2: 40 / 32, 6: 37 / 32, 7: 37 / 32, 4: 6, 5: 6, 8: 11, 3: 6}
+# DRAM bytes per prime of residue_kernel<PROTH> from one ncu capture on
+# [2^32, 2^32 + 2^27): 48,436,480 + 1,024 bytes for 6,047,768 primes; each
+# prime is read once per launch, so a full launch's traffic is this figure
+# times its primes
+DRAM_BYTES_PER_PRIME = (48436480 + 1024) / 6047768
 
 
 def mv_bound(y: int) -> int:
@@ -125,57 +173,47 @@ def measured_peaks() -> dict:
         return {}
 
 
-def int_peak(device: int):
-    """Integer ALU instructions/s from libctd_probe.so (measured on this GPU now)."""
-    from cutrialdive_gb300._build import PROBE
-
-    if not os.path.exists(PROBE):
-        return None
-    L = ctypes.CDLL(PROBE)
-    L.ctd_probe_int_peak.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
-    best = 0.0
-    for _ in range(3):
-        v, s = ctypes.c_double(), ctypes.c_double()
-        if L.ctd_probe_int_peak(device, ctypes.byref(v), ctypes.byref(s)) == 0:
-            best = max(best, v.value)
-    return best or None
-
-
 # ---------------------------------------------------------------- CPU legs
-def cpu_updates_per_s(n_primes_target_s: float, threads: int, lo: int):
+def cpu_updates_per_s(wl: Plain, target_s: float, threads: int, lo: int):
     """Times the CPU oracle's residue loop (the reference CPU engine's
-    process_chunk, restated) on a prime sample starting at `lo` sized for
-    about `n_primes_target_s` seconds.  Returns (updates/s, sample text)."""
+    process_chunk, restated) over every job of the workload on a prime sample
+    starting at `lo`, sized for about `target_s` seconds.
+    Returns (updates/s, updates, seconds, sample text)."""
     import oracle
 
-    N = N1 - N0
-    # calibrate on a small slice
-    width = 1 << 18
+    lo = max(lo, 3)
+    terms = sum(n1 - n0 for _, _, n0, n1 in wl.jobs)
+
+    def run(primes):
+        t = time.perf_counter()
+        for fam, param, n0, n1 in wl.jobs:
+            oracle.residue_hits(fam, param, n0, n1, primes, MAXF, threads=threads)
+        return time.perf_counter() - t
+
+    width = 1 << 16
     primes = oracle.sieve(lo, lo + width)
-    t = time.perf_counter()
-    oracle.residue_hits(FAMILY, PARAM, N0, N1, primes, MAXF, threads=threads)
-    dt = max(time.perf_counter() - t, 1e-3)
-    rate = primes.size * N / dt
-    want = n_primes_target_s * rate / N  # primes
+    dt = max(run(primes), 1e-3)
+    want = target_s * (primes.size / dt)  # primes
     width = max(width, int(width * want / max(primes.size, 1)))
     primes = oracle.sieve(lo, lo + width)
-    t = time.perf_counter()
-    oracle.residue_hits(FAMILY, PARAM, N0, N1, primes, MAXF, threads=threads)
-    dt = time.perf_counter() - t
-    return primes.size * N / dt, primes.size * N, dt, f"primes in [{lo}, {lo + width}) ({primes.size}), n in [1, 100001)"
+    dt = run(primes)
+    jobs = ", ".join(f"{FAMILY_NAMES[f].lower()} n in [{a}, {b})" for f, _, a, b in wl.jobs)
+    return (primes.size * terms / dt, primes.size * terms, dt,
+            f"primes in [{lo}, {lo + width}) ({primes.size}) x ({jobs})")
 
 
 def run_reference(args, world, rank):
     if rank != 0:
         return 0
+    wl = PLAIN[args.workload] if args.workload in PLAIN else PLAIN["proth"]
     threads = os.cpu_count() or 1
     import oracle  # noqa: F401  (fails loudly if missing)
 
     per_step_s = 2.0
     total_updates, total_t, samples = 0, 0.0, []
     for i in range(args.warmup + args.steps):
-        lo = F0 + (i % NSEG) * SEG
-        rate, updates, dt, sample = cpu_updates_per_s(per_step_s, threads, lo)
+        lo, _ = wl.segment(i)
+        rate, updates, dt, sample = cpu_updates_per_s(wl, per_step_s, threads, lo)
         if i >= args.warmup:
             total_updates += updates
             total_t += dt
@@ -186,15 +224,39 @@ def run_reference(args, world, rank):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic (deterministic: the configuration has no random input)",
-        "config": {"workload": WORKLOAD, "step": "a bounded sample of one 2^30 prime segment (about 2 s of CPU)"},
+        "config": {"workload": wl.text,
+                   "step": f"a bounded sample (about {per_step_s:g} s of CPU) of one 2^{wl.seg_bits} prime segment"},
         "cpu_baseline": {"value": value, "unit": "updates/s", "cores": threads, "kind": "port",
                          "sample": samples[0] if samples else ""},
         "e2e": {"value": value, "unit": "updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": ("the reference CPU engine (src/trial_factoring_impl.hpp:193-366) as restated by the oracle; "
-                 "the reference's own build (oracle/_ref) is x86-only and does not travel to this host"),
+        "note": ("the reference CPU engine (src/trial_factoring_impl.hpp:193-366) as restated by the oracle, all host "
+                 "threads; the reference's own build (oracle/_ref) is x86-only and does not travel to this host"),
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def probe_peaks(device: int) -> dict:
+    """Integer roofline denominators measured now by libctd_probe.so: the
+    ALU-pipe compare rate and the mixed add/xor integer rate."""
+    from cutrialdive_gb300._build import PROBE
+
+    out = {"alu": None, "int": None}
+    if not os.path.exists(PROBE):
+        return out
+    L = ctypes.CDLL(PROBE)
+    for key, fn in (("alu", "ctd_probe_alu_peak"), ("int", "ctd_probe_int_peak")):
+        f = getattr(L, fn, None)
+        if f is None:
+            continue
+        f.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+        best = 0.0
+        for _ in range(3):
+            v, s = ctypes.c_double(), ctypes.c_double()
+            if f(device, ctypes.byref(v), ctypes.byref(s)) == 0:
+                best = max(best, v.value)
+        out[key] = best or None
+    return out
 
 
 # --------------------------------------------------------------- GPU leg
@@ -205,6 +267,10 @@ def run_ours(args, world, rank, local):
     import cutrialdive_gb300 as ctd
     from cutrialdive_gb300 import _native as NAT
 
+    wl = PLAIN[args.workload]
+    if args.segment_bits:
+        wl.seg_bits = args.segment_bits
+    steps = args.steps if args.steps else wl.default_steps
     torch.cuda.set_device(local)
     if world > 1:
         import torch.distributed as dist
@@ -215,35 +281,48 @@ def run_ours(args, world, rank, local):
     info = eng.device_info()
     stream = torch.cuda.Stream(device=local)
     sptr = ctypes.c_void_p(stream.cuda_stream)
-    N = N1 - N0
-    cap = mv_bound(SEG)
+    cap = mv_bound(wl.seg)
     primes = torch.empty(cap, dtype=torch.int64, device="cuda")
-    counts = torch.zeros(N, dtype=torch.int32, device="cuda")
-    factors = torch.zeros(N * MAXF, dtype=torch.int64, device="cuda")
-    job = NAT.CtdJob(FAMILY, MAXF, PARAM, N0, N1, F0, F1)
+    bufs = []
+    for fam, param, n0, n1 in wl.jobs:
+        N = n1 - n0
+        bufs.append((torch.zeros(N, dtype=torch.int32, device="cuda"),
+                     torch.zeros(N * MAXF, dtype=torch.int64, device="cuda")))
+    terms = [n1 - n0 for _, _, n0, n1 in wl.jobs]
     count = ctypes.c_uint64()
 
+    def check(rc):
+        if rc:
+            raise NAT.CtdError(rc, L.ctd_last_error(eng.handle).decode())
+
     def seg_of(j):
-        return (rank * args.steps + j) % NSEG
+        return wl.segment(rank * steps + j)
 
     def step(j, ev=None):
-        fx = F0 + seg_of(j) * SEG
+        """One segment for every job; returns the primes tested (the prime 2 included)."""
+        fx, fy = seg_of(j)
         with torch.cuda.stream(stream):
             if ev is not None:
                 ev[0].record(stream)
-            rc = L.ctd_sieve_device(eng.handle, fx, fx + SEG, ctypes.c_void_p(primes.data_ptr()), cap,
-                                    ctypes.byref(count), sptr)
-            if rc:
-                raise NAT.CtdError(rc, L.ctd_last_error(eng.handle).decode())
+            extra = 0
+            if fx <= 2 < fy:
+                for (fam, param, n0, n1), (c, f) in zip(wl.jobs, bufs):
+                    job = NAT.CtdJob(fam, MAXF, param, n0, n1, 2, fy)
+                    check(L.ctd_mod2_device(eng.handle, ctypes.byref(job), ctypes.c_void_p(c.data_ptr()),
+                                            ctypes.c_void_p(f.data_ptr()), sptr))
+                extra, fx = 1, 3
+            check(L.ctd_sieve_device(eng.handle, fx, fy, ctypes.c_void_p(primes.data_ptr()), cap,
+                                     ctypes.byref(count), sptr))
             if ev is not None:
                 ev[1].record(stream)
-            rc = L.ctd_residues_device(eng.handle, ctypes.byref(job), ctypes.c_void_p(primes.data_ptr()), count.value,
-                                       ctypes.c_void_p(counts.data_ptr()), ctypes.c_void_p(factors.data_ptr()), sptr)
-            if rc:
-                raise NAT.CtdError(rc, L.ctd_last_error(eng.handle).decode())
-            if ev is not None:
-                ev[2].record(stream)
-        return count.value
+            for k, ((fam, param, n0, n1), (c, f)) in enumerate(zip(wl.jobs, bufs)):
+                job = NAT.CtdJob(fam, MAXF, param, n0, n1, fx, fy)
+                check(L.ctd_residues_device(eng.handle, ctypes.byref(job), ctypes.c_void_p(primes.data_ptr()),
+                                            count.value, ctypes.c_void_p(c.data_ptr()), ctypes.c_void_p(f.data_ptr()),
+                                            sptr))
+                if ev is not None:
+                    ev[2 + k].record(stream)
+        return count.value + extra, count.value
 
     def barrier():
         if world > 1:
@@ -253,25 +332,28 @@ def run_ours(args, world, rank, local):
         step(j)
     torch.cuda.synchronize()
 
-    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    nj = len(wl.jobs)
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(2 + nj)] for _ in range(steps)]
     t_start = torch.cuda.Event(enable_timing=True)
     t_end = torch.cuda.Event(enable_timing=True)
     launches0 = L.ctd_kernel_launches()
     barrier()
     torch.cuda.synchronize()
-    nprimes = []
+    nprimes, nodd = [], []
     with ClockSampler(local) as clocks:
         t_start.record(stream)
-        for j in range(args.steps):
-            nprimes.append(step(j, evs[j]))
+        for j in range(steps):
+            a, b = step(j, evs[j])
+            nprimes.append(a)
+            nodd.append(b)
         t_end.record(stream)
         torch.cuda.synchronize()
     barrier()
     launches = L.ctd_kernel_launches() - launches0
     elapsed = t_start.elapsed_time(t_end) * 1e-3
     sieve_ms = [e[0].elapsed_time(e[1]) for e in evs]
-    resid_ms = [e[1].elapsed_time(e[2]) for e in evs]
-    updates = sum(nprimes) * N
+    job_ms = [[evs[j][1 + k].elapsed_time(evs[j][2 + k]) for j in range(steps)] for k in range(nj)]
+    updates = sum(nprimes) * sum(terms)
     if world > 1:
         t = torch.tensor([elapsed, float(updates)], dtype=torch.float64, device="cuda")
         tmax = t.clone()
@@ -285,79 +367,99 @@ def run_ours(args, world, rank, local):
     # ---- end to end: the C-ABI plain call with host buffers, copies inside
     e2e = None
     if not args.no_e2e:
-        hc = torch.zeros(N, dtype=torch.int32).pin_memory()
-        hf = torch.zeros(N * MAXF, dtype=torch.int64).pin_memory()
-        buf = ctd.factors_buffer(N0, MAXF, hc.numpy().view(np.uint32), hf.numpy().view(np.uint64))
-        e2e_updates = 0
-        for j in range(min(args.warmup, 1)):
-            fx = F0 + seg_of(j) * SEG
-            eng.run_plain(NAT.CtdJob(FAMILY, MAXF, PARAM, N0, N1, fx, fx + SEG), buf, segment_length=SEG)
+        hbufs = []
+        for (fam, param, n0, n1) in wl.jobs:
+            N = n1 - n0
+            hc = torch.zeros(N, dtype=torch.int32).pin_memory()
+            hf = torch.zeros(N * MAXF, dtype=torch.int64).pin_memory()
+            hbufs.append(ctd.factors_buffer(n0, MAXF, hc.numpy().view(np.uint32), hf.numpy().view(np.uint64)))
+
+        def e2e_step(j):
+            fx, fy = seg_of(j)
+            for (fam, param, n0, n1), buf in zip(wl.jobs, hbufs):
+                eng.run_plain(NAT.CtdJob(fam, MAXF, param, n0, n1, fx, fy), buf, segment_length=wl.seg)
+
+        e2e_step(0)
         barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for j in range(args.steps):
-            fx = F0 + seg_of(j) * SEG
-            eng.run_plain(NAT.CtdJob(FAMILY, MAXF, PARAM, N0, N1, fx, fx + SEG), buf, segment_length=SEG)
-            e2e_updates += nprimes[j] * N
+        for j in range(steps):
+            e2e_step(j)
         torch.cuda.synchronize()
         e2e_t = time.perf_counter() - t0
         barrier()
-        e2e_total = float(e2e_updates)
+        e2e_total = float(updates)
         if world > 1:
             t = torch.tensor([e2e_t, e2e_total], dtype=torch.float64, device="cuda")
             tmax = t.clone()
             torch.distributed.all_reduce(tmax[:1], op=torch.distributed.ReduceOp.MAX)
             torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
             e2e_t, e2e_total = float(tmax[0]), float(t[1])
-        e2e = {"value": e2e_total / e2e_t, "unit": "updates/s", "h2d_bytes_per_step": N * 4 + N * MAXF * 8,
-               "d2h_bytes_per_step": N * 4 + N * MAXF * 8,
-               "api": "ctd_run_plain (include/ctd_gpu.h) with pinned host factors buffers, one segment per call"}
+        hbytes = sum(N * (4 + 8 * MAXF) for N in terms)
+        e2e = {"value": e2e_total / e2e_t, "unit": "updates/s", "h2d_bytes_per_step": hbytes,
+               "d2h_bytes_per_step": hbytes,
+               "api": "ctd_run_plain (include/ctd_gpu.h) per job with pinned host factors buffers, one segment per call"}
 
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
         return 0
 
-    peak_int = int_peak(local)
-    res_avg_s = statistics.mean(resid_ms) * 1e-3
-    per_launch_updates = statistics.mean(nprimes) * N
-    achieved = per_launch_updates * OPS_PER_UPDATE / res_avg_s
+    peaks = probe_peaks(local)
+    # the dominant kernel of the step and its roofline
+    k = max(range(nj), key=lambda i: sum(job_ms[i]))
+    fam = wl.jobs[k][0]
+    launch_s = statistics.mean(job_ms[k]) * 1e-3
+    per_launch_updates = statistics.mean(nodd) * terms[k]
+    ops = ALU_OPS_PER_UPDATE[fam]
+    achieved = per_launch_updates * ops / launch_s
     roofline = {
-        "bound": "int_alu", "kernel": "residue_kernel<PROTH>",
-        "achieved": achieved / 1e9, "peak": (peak_int / 1e9) if peak_int else None, "unit": "Gop/s",
-        "frac": (achieved / peak_int) if peak_int else None,
-        "traffic": DRAM_BYTES_PER_PRIME * statistics.mean(nprimes),
-        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a 2^27-segment launch, "
-                          "scaled by primes per launch (profiles/residue_kernel_proth_k3_seg2p27_full.md)",
-        "algorithmic_bytes": 8 * statistics.mean(nprimes),
-        "ops_per_update": OPS_PER_UPDATE, "launch_ms": statistics.mean(resid_ms),
-        "peak_source": "measured now: libctd_probe 32-bit add/xor chains (integer ALU issue rate) on this GPU",
+        "bound": "int_alu", "kernel": f"residue_kernel<{FAMILY_NAMES[fam]}>",
+        "achieved": achieved / 1e9, "peak": (peaks["alu"] / 1e9) if peaks["alu"] else None, "unit": "Gop/s",
+        "frac": (achieved / peaks["alu"]) if peaks["alu"] else None,
+        "ops_per_update": ops, "launch_ms": launch_s * 1e3,
+        "peak_source": "measured now: libctd_probe predicate-compare chains (integer ALU pipe) on this GPU",
+        "int_issue_peak": (peaks["int"] / 1e9) if peaks["int"] else None,
+        "kernel_share": sum(job_ms[k]) / max(sum(sum(x) for x in job_ms) + sum(sieve_ms), 1e-9),
     }
+    if fam == 1:
+        roofline["traffic"] = DRAM_BYTES_PER_PRIME * statistics.mean(nodd)
+        roofline["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of a 2^27-segment launch, "
+                                      "scaled by primes per launch (profiles/residue_kernel_proth_k3_seg2p27_full.md)")
+    else:
+        roofline["traffic"] = None
+    roofline["algorithmic_bytes"] = 8 * statistics.mean(nodd)
+    per_job = {f"{FAMILY_NAMES[f].lower()}": {"ms_per_launch": statistics.mean(job_ms[i]),
+                                             "updates_per_s": statistics.mean(nodd) * terms[i] /
+                                             (statistics.mean(job_ms[i]) * 1e-3)}
+               for i, (f, _, _, _) in enumerate(wl.jobs)}
     sieve_s = statistics.mean(sieve_ms) * 1e-3
-    peaks = measured_peaks()
-    hbm = peaks.get("hbm_gbs")
-    sieve_bytes = statistics.mean(nprimes) * 8
+    hbm = measured_peaks().get("hbm_gbs")
+    sieve_bytes = statistics.mean(nodd) * 8
     sieve = {"kernel": "device sieve (sieve_windows + scan_counts + compact_windows, host count readback)",
-             "ms_per_step": statistics.mean(sieve_ms), "primes_per_step": statistics.mean(nprimes),
+             "ms_per_step": statistics.mean(sieve_ms), "primes_per_step": statistics.mean(nodd),
              "achieved_gbs": sieve_bytes / sieve_s / 1e9, "peak_gbs": hbm,
              "frac": (sieve_bytes / sieve_s / 1e9 / hbm) if hbm else None,
              "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if hbm else "absent"}
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        rate, _, dt, sample = cpu_updates_per_s(15.0, threads, F0)
+        rate, _, dt, sample = cpu_updates_per_s(wl, 15.0, threads, wl.f0)
         cpu = {"value": rate, "unit": "updates/s", "cores": threads, "kind": "port", "sample": sample,
                "seconds": dt}
     line = {
-        "metric": METRIC, "value": value, "unit": "updates/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
+        "metric": METRIC, "value": value, "unit": "updates/s", "n_gpus": world, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic (deterministic: the configuration has no random input)",
-        "config": {"workload": WORKLOAD, "step": "one 2^30-wide prime segment: device sieve + residue kernel",
-                   "segments": NSEG, "max_factors_per_number": MAXF,
-                   "l2": "inputs larger than L2 (about 370 MB of primes per step)",
+        "config": {"workload": wl.text,
+                   "step": f"one 2^{wl.seg_bits}-wide prime segment: device sieve + one residue launch per job",
+                   "segments": wl.nseg, "max_factors_per_number": MAXF,
+                   "l2": f"inputs larger than L2 (about {8 * statistics.mean(nodd) / 1e6:.0f} MB of primes per step)"
+                         if 8 * statistics.mean(nodd) > 129e6 else
+                         "the whole prime list of a step is read once per job launch",
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU", "device": info["name"]},
-        "roofline": roofline, "sieve": sieve, "cpu_baseline": cpu, "e2e": e2e,
+        "roofline": roofline, "per_job": per_job, "sieve": sieve, "cpu_baseline": cpu, "e2e": e2e,
         "clocks": clocks.summary(), "gpu_launches": int(launches),
         "updates": total_updates, "seconds": elapsed,
     }
@@ -528,25 +630,27 @@ def run_served(args, world, rank, local):
 
 
 def main() -> int:
-    global SEG, NSEG
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=NSEG, help="steps (default: every 2^30 segment once)")
+    ap.add_argument("--steps", type=int, default=0,
+                    help="timed steps (default: proth 12 = every 2^30 segment of [2^32, 2^34) once; linear 3; "
+                         "smarandache 12; batched 3)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--segment-bits", type=int, default=30,
+    ap.add_argument("--segment-bits", type=int, default=0,
                     help="log2 of the prime-segment width of one step (profiling uses smaller cases)")
-    ap.add_argument("--workload", choices=["proth", "batched", "served"], default="proth",
-                    help="proth: the plain single-job line (default); batched: the 64-job mix through "
-                         "ctd_batch_run against the same jobs one by one; served: the Poisson serving sweep")
+    ap.add_argument("--workload", choices=["proth", "linear", "smarandache", "batched", "served"], default="proth",
+                    help="proth: the plain single-job line (default); linear: Fibonacci, Lucas and tribonacci back "
+                         "to back; smarandache: the CPU-runnable plain configuration; batched: the 64-job mix "
+                         "through ctd_batch_run against the same jobs one by one; served: the Poisson serving sweep")
     ap.add_argument("--shrink", type=int, default=256, help="batched/served: keep the first 1/shrink of each TF range")
     ap.add_argument("--rates", default="1,5,10,25,50", help="served: arrival rates in jobs/s")
     ap.add_argument("--window", type=float, default=10.0, help="served: seconds of arrivals per rate")
     args = ap.parse_args()
-    SEG = 1 << args.segment_bits
-    NSEG = (F1 - F0) // SEG
+    if not args.steps:
+        args.steps = PLAIN[args.workload].default_steps if args.workload in PLAIN else 3
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     world, rank, local = dist_env()

@@ -1,4 +1,4 @@
-// ctd_probe.cu -- measurement probe for the roofline denominator (bench only).
+// ctd_probe.cu -- measurement probes for the roofline denominators (bench only).
 //
 // The residue kernels are bound by the 32-bit integer ALU issue rate, which
 // MEASURED_PEAKS-style copy/GEMM peaks do not describe.  This kernel runs
@@ -35,9 +35,81 @@ __global__ void __launch_bounds__(256) int_chains(uint32_t *out, uint32_t iters,
         out[blockIdx.x] = s;
 }
 
+// Integer ALU pipe alone: predicate-accumulating compares (ISETP with an OR
+// into the destination predicate), which only the ALU pipe executes -- the
+// instruction the compare-bound residue walks are made of.  Eight
+// independent predicate chains of 32 compares per iteration.
+__global__ void __launch_bounds__(256) isetp_chains(uint32_t *out, uint32_t iters, uint32_t y)
+{
+    uint32_t a = threadIdx.x * 0x9e3779b9u + y, flags = 0;
+    for (uint32_t i = 0; i < iters; ++i) {
+        uint32_t f;
+        asm volatile(
+            "{\n\t.reg .pred q<8>;\n\t"
+            "setp.eq.u32 q0, %1, %2;\n\tsetp.eq.u32 q1, %1, %3;\n\tsetp.eq.u32 q2, %1, %4;\n\t"
+            "setp.eq.u32 q3, %1, %5;\n\tsetp.eq.u32 q4, %1, %6;\n\tsetp.eq.u32 q5, %1, %7;\n\t"
+            "setp.eq.u32 q6, %1, %8;\n\tsetp.eq.u32 q7, %1, %9;\n\t"
+#define CTD_PROBE_8                                                                                          \
+            "setp.eq.or.u32 q0, %1, %9, q0;\n\tsetp.eq.or.u32 q1, %1, %8, q1;\n\t"                        \
+            "setp.eq.or.u32 q2, %1, %7, q2;\n\tsetp.eq.or.u32 q3, %1, %6, q3;\n\t"                        \
+            "setp.eq.or.u32 q4, %1, %5, q4;\n\tsetp.eq.or.u32 q5, %1, %4, q5;\n\t"                        \
+            "setp.eq.or.u32 q6, %1, %3, q6;\n\tsetp.eq.or.u32 q7, %1, %2, q7;\n\t"
+            CTD_PROBE_8 CTD_PROBE_8 CTD_PROBE_8
+#undef CTD_PROBE_8
+            "or.pred q0, q0, q1;\n\tor.pred q2, q2, q3;\n\tor.pred q4, q4, q5;\n\tor.pred q6, q6, q7;\n\t"
+            "or.pred q0, q0, q2;\n\tor.pred q4, q4, q6;\n\tor.pred q0, q0, q4;\n\t"
+            "selp.u32 %0, 1, 0, q0;\n\t}"
+            : "=r"(f)
+            : "r"(a), "r"(y), "r"(y + 1), "r"(y + 2), "r"(y + 3), "r"(y + 4), "r"(y + 5), "r"(y + 6), "r"(y + 7));
+        flags |= f;
+        a += 0x61c88647u;
+    }
+    if (flags == 0x12345678u)  // never: keeps the compares live
+        out[blockIdx.x] = flags;
+}
+
 }  // namespace
 
 extern "C" {
+
+// Predicate compares per second (ALU pipe) over a ~0.5 s run on `device`
+// (32 compares per iteration; the few or/select/add instructions around them
+// are not counted, so this slightly understates the pipe).  Returns 0 on
+// success.
+int ctd_probe_alu_peak(int device, double *compares_per_s, double *seconds)
+{
+    if (cudaSetDevice(device) != cudaSuccess)
+        return -2;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    uint32_t *out = nullptr;
+    const int block = 256, grid = sms * 8;
+    if (cudaMalloc(&out, grid * sizeof(uint32_t)) != cudaSuccess)
+        return -3;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const uint32_t iters = 1 << 14;
+    isetp_chains<<<grid, block>>>(out, 64, 0x1234567u);  // warm-up
+    cudaEventRecord(e0);
+    const int reps = 8;
+    for (int r = 0; r < reps; ++r)
+        isetp_chains<<<grid, block>>>(out, iters, 0x1234567u + 16 * r);
+    cudaEventRecord(e1);
+    cudaError_t err = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (err != cudaSuccess || ms <= 0.f)
+        return -2;
+    const double instr = 32.0 * (double)iters * block * grid * reps;
+    *compares_per_s = instr / (ms * 1e-3);
+    if (seconds)
+        *seconds = ms * 1e-3;
+    return 0;
+}
 
 // Integer ALU instructions per second over a ~0.5 s run on `device`
 // (2 instructions x 8 chains x 16 unrolled x iters per thread).  Returns 0

@@ -195,6 +195,29 @@ constexpr int BS = 32;
 // halving mod odd p < 2^63: x/2 or (x + p)/2
 __device__ __forceinline__ uint64_t half63(uint64_t x, uint64_t p) { return (x + ((x & 1) ? p : 0)) >> 1; }
 
+// Nonzero iff lo equals one of t[k .. k+15]: sixteen predicate-accumulating
+// compares in four independent chains (one ALU instruction each).
+__device__ __forceinline__ uint32_t match16(uint32_t lo, const uint32_t (&t)[BS], int k)
+{
+    uint32_t f;
+    asm("{\n\t.reg .pred c<4>;\n\t"
+        "setp.eq.u32 c0, %1, %2;\n\tsetp.eq.u32 c1, %1, %3;\n\t"
+        "setp.eq.u32 c2, %1, %4;\n\tsetp.eq.u32 c3, %1, %5;\n\t"
+        "setp.eq.or.u32 c0, %1, %6, c0;\n\tsetp.eq.or.u32 c1, %1, %7, c1;\n\t"
+        "setp.eq.or.u32 c2, %1, %8, c2;\n\tsetp.eq.or.u32 c3, %1, %9, c3;\n\t"
+        "setp.eq.or.u32 c0, %1, %10, c0;\n\tsetp.eq.or.u32 c1, %1, %11, c1;\n\t"
+        "setp.eq.or.u32 c2, %1, %12, c2;\n\tsetp.eq.or.u32 c3, %1, %13, c3;\n\t"
+        "setp.eq.or.u32 c0, %1, %14, c0;\n\tsetp.eq.or.u32 c1, %1, %15, c1;\n\t"
+        "setp.eq.or.u32 c2, %1, %16, c2;\n\tsetp.eq.or.u32 c3, %1, %17, c3;\n\t"
+        "or.pred c0, c0, c1;\n\tor.pred c2, c2, c3;\n\tor.pred c0, c0, c2;\n\t"
+        "selp.u32 %0, 1, 0, c0;\n\t}"
+        : "=r"(f)
+        : "r"(lo), "r"(t[k]), "r"(t[k + 1]), "r"(t[k + 2]), "r"(t[k + 3]), "r"(t[k + 4]), "r"(t[k + 5]),
+          "r"(t[k + 6]), "r"(t[k + 7]), "r"(t[k + 8]), "r"(t[k + 9]), "r"(t[k + 10]), "r"(t[k + 11]),
+          "r"(t[k + 12]), "r"(t[k + 13]), "r"(t[k + 14]), "r"(t[k + 15]));
+    return f;
+}
+
 // Tests the terms idx .. idx + nblk*BS - 1 of u -> 2u (DOUBLE) or
 // u -> u + c, starting from state u at idx; returns the state at
 // idx + nblk*BS.  tlo[j] = low word of the j-step target; W = the giant step
@@ -207,15 +230,7 @@ __device__ __forceinline__ uint64_t bsgs_blocks(const Mont &m, uint64_t u, uint6
     const uint64_t p = m.p;
     for (uint64_t b = 0; b < nblk; ++b) {
         const uint32_t lo = (uint32_t)u;
-        bool c0 = false, c1 = false, c2 = false, c3 = false;
-#pragma unroll
-        for (int j = 0; j < BS; j += 4) {
-            c0 |= lo == tlo[j];
-            c1 |= lo == tlo[j + 1];
-            c2 |= lo == tlo[j + 2];
-            c3 |= lo == tlo[j + 3];
-        }
-        if (c0 | c1 | c2 | c3) {
+        if (match16(lo, tlo, 0) | match16(lo, tlo, 16)) {
             uint64_t v = u;
 #pragma unroll 1
             for (int j = 0; j < BS; ++j) {
