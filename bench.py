@@ -79,17 +79,18 @@ FAMILY_NAMES = {0: "MERSENNE", 1: "PROTH", 2: "RIESEL", 3: "SMARANDACHE", 4: "FI
 # Algorithmic integer-ALU operations per update, by family (32-bit ops of the
 # exact algorithm the kernel runs; multiplies, which go to the multiply pipe,
 # are listed separately):
-#  * doubling (Proth/Riesel/Mersenne) and fixed-n: baby-step/giant-step
-#    blocks of 32 terms: 32 low-word compares + the giant step's adds and
-#    compares (8 for a Montgomery multiplication, 5 for a modular add) per
-#    block -> 40/32 and 37/32;
+#  * doubling (Proth/Riesel/Mersenne): baby-step/giant-step blocks of 32
+#    terms walked backwards: 32 low-word compares per block, the giant step
+#    (u 2^-32, a 32-bit Montgomery reduction) is 4 multiply-pipe
+#    instructions -> 32/32 ALU ops;
+#  * fixed-n: the same blocks, giant step a modular add (5 ALU ops) -> 37/32;
 #  * Fibonacci/Lucas: modular add (2 add, 1 sign test, 2 predicated add) +
 #    1 compare = 6;
 #  * tribonacci: two-term add and -2p (4), two sign tests and predicated
 #    adds (6), compare (1) = 11;
 #  * Smarandache (64-bit Shoup): adds/subtracts of x M + m - q p (4) and
 #    two low-word compares = 6, plus 9 32-bit multiplies.
-ALU_OPS_PER_UPDATE = {0: 40 / 32, 1: 40 / 32, 2: 40 / 32, 6: 37 / 32, 7: 37 / 32, 4: 6, 5: 6, 8: 11, 3: 6}
+ALU_OPS_PER_UPDATE = {0: 32 / 32, 1: 32 / 32, 2: 32 / 32, 6: 37 / 32, 7: 37 / 32, 4: 6, 5: 6, 8: 11, 3: 6}
 # DRAM bytes per prime of residue_kernel<PROTH> from one ncu capture on
 # [2^32, 2^32 + 2^27): 48,436,480 + 1,024 bytes for 6,047,768 primes; each
 # prime is read once per launch, so a full launch's traffic is this figure

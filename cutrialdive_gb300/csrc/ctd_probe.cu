@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(256) int_chains(uint32_t *out, uint32_t iters,
 // Integer ALU pipe alone: predicate-accumulating compares (ISETP with an OR
 // into the destination predicate), which only the ALU pipe executes -- the
 // instruction the compare-bound residue walks are made of.  Eight
-// independent predicate chains of 32 compares per iteration.
+// independent predicate chains, 128 compares per iteration.
 __global__ void __launch_bounds__(256) isetp_chains(uint32_t *out, uint32_t iters, uint32_t y)
 {
     uint32_t a = threadIdx.x * 0x9e3779b9u + y, flags = 0;
@@ -54,7 +54,8 @@ __global__ void __launch_bounds__(256) isetp_chains(uint32_t *out, uint32_t iter
             "setp.eq.or.u32 q2, %1, %7, q2;\n\tsetp.eq.or.u32 q3, %1, %6, q3;\n\t"                        \
             "setp.eq.or.u32 q4, %1, %5, q4;\n\tsetp.eq.or.u32 q5, %1, %4, q5;\n\t"                        \
             "setp.eq.or.u32 q6, %1, %3, q6;\n\tsetp.eq.or.u32 q7, %1, %2, q7;\n\t"
-            CTD_PROBE_8 CTD_PROBE_8 CTD_PROBE_8
+            CTD_PROBE_8 CTD_PROBE_8 CTD_PROBE_8 CTD_PROBE_8 CTD_PROBE_8 CTD_PROBE_8 CTD_PROBE_8 CTD_PROBE_8
+            CTD_PROBE_8 CTD_PROBE_8 CTD_PROBE_8 CTD_PROBE_8 CTD_PROBE_8 CTD_PROBE_8 CTD_PROBE_8
 #undef CTD_PROBE_8
             "or.pred q0, q0, q1;\n\tor.pred q2, q2, q3;\n\tor.pred q4, q4, q5;\n\tor.pred q6, q6, q7;\n\t"
             "or.pred q0, q0, q2;\n\tor.pred q4, q4, q6;\n\tor.pred q0, q0, q4;\n\t"
@@ -73,9 +74,9 @@ __global__ void __launch_bounds__(256) isetp_chains(uint32_t *out, uint32_t iter
 extern "C" {
 
 // Predicate compares per second (ALU pipe) over a ~0.5 s run on `device`
-// (32 compares per iteration; the few or/select/add instructions around them
-// are not counted, so this slightly understates the pipe).  Returns 0 on
-// success.
+// (128 compares per iteration; the dozen or/select/add/loop instructions
+// around them are not counted, so this understates the pipe by a few
+// percent).  Returns 0 on success.
 int ctd_probe_alu_peak(int device, double *compares_per_s, double *seconds)
 {
     if (cudaSetDevice(device) != cudaSuccess)
@@ -89,7 +90,7 @@ int ctd_probe_alu_peak(int device, double *compares_per_s, double *seconds)
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    const uint32_t iters = 1 << 14;
+    const uint32_t iters = 1 << 12;
     isetp_chains<<<grid, block>>>(out, 64, 0x1234567u);  // warm-up
     cudaEventRecord(e0);
     const int reps = 8;
@@ -104,7 +105,7 @@ int ctd_probe_alu_peak(int device, double *compares_per_s, double *seconds)
     cudaFree(out);
     if (err != cudaSuccess || ms <= 0.f)
         return -2;
-    const double instr = 32.0 * (double)iters * block * grid * reps;
+    const double instr = 128.0 * (double)iters * block * grid * reps;
     *compares_per_s = instr / (ms * 1e-3);
     if (seconds)
         *seconds = ms * 1e-3;

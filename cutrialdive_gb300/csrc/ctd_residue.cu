@@ -31,10 +31,23 @@ uint64_t kernel_launch_count() { return g_launches.load(std::memory_order_relaxe
 // ----------------------------------------------------------------- push
 // factors_buffer push (src/device_factors_buffer.hpp:119-129): atomic slot
 // reservation, store only below the per-term capacity; the count keeps
-// growing so overflow is visible to the host.
+// growing so overflow is visible to the host.  Warp-aggregated: the lanes
+// that push to the same term at the same time (every prime divides a zero
+// term such as T(1)) are grouped with a match, their leader reserves all
+// their slots with one atomic, and each lane stores at its rank -- one
+// atomic per (warp, term) instead of one per lane.  Slot order stays the
+// order of reservation, as in the reference.
 __device__ __forceinline__ void push(const FactorsView &fb, uint64_t idx, uint64_t p)
 {
-    uint32_t pos = atomicAdd(&fb.counts[idx], 1u);
+    const uint32_t active = __activemask();
+    const uint32_t peers = __match_any_sync(active, (unsigned long long)idx);
+    const uint32_t lane = threadIdx.x & 31u;
+    const int leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if ((int)lane == leader)
+        base = atomicAdd(&fb.counts[idx], (uint32_t)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    const uint32_t pos = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
     if (pos < fb.max_factors)
         fb.factors[idx * fb.max_factors + pos] = p;
 }
@@ -218,6 +231,20 @@ __device__ __forceinline__ uint32_t match16(uint32_t lo, const uint32_t (&t)[BS]
     return f;
 }
 
+// u * 2^-32 mod p for u < p, odd p < 2^63: one 32-bit Montgomery reduction,
+// m = u_lo (-p^-1) mod 2^32, r = (u + m p) / 2^32.  u + m p = 0 mod 2^32 and
+// r < (p + 2^32 p) / 2^32, so r < p with no final subtraction; every step is
+// a 32x32(+64) multiply-add on the multiply pipe (`one` is 1, passed at run
+// time so the last add stays a multiply-add).
+__device__ __forceinline__ uint64_t redc32(uint64_t u, uint32_t plo, uint32_t phi, uint32_t pinv32, uint32_t one)
+{
+    const uint32_t ulo = (uint32_t)u, uhi = (uint32_t)(u >> 32);
+    const uint32_t m = ulo * pinv32;
+    const uint64_t t1 = (uint64_t)m * plo + ulo;  // low word 0; high word carries
+    const uint64_t h = (uint64_t)(uint32_t)(t1 >> 32) * one + uhi;
+    return (uint64_t)m * phi + h;
+}
+
 // Tests the terms idx .. idx + nblk*BS - 1 of u -> 2u (DOUBLE) or
 // u -> u + c, starting from state u at idx; returns the state at
 // idx + nblk*BS.  tlo[j] = low word of the j-step target; W = the giant step
@@ -268,6 +295,20 @@ __device__ __forceinline__ void run_doubling(const JobView &job, uint64_t p, uin
     const uint64_t steps = e - s - 1;
     const uint64_t nblk = (e - s) / BS;
     if (p < (1ull << 63) && nblk >= 2) {
+        // blocks walked backwards: the giant step u -> u 2^-32 is one
+        // reduction on the multiply pipe (redc32).  Start from the state at
+        // the end of the last whole block, walk the short tail forwards.
+        const uint64_t ts = s + nblk * BS;
+        const uint64_t UT = m.pow2(ts);
+        uint64_t ut;
+        if (FAM == MERSENNE) {
+            ut = m.from(UT);
+        } else {
+            const uint64_t k = job.param < p ? job.param : job.param % p;
+            ut = m.mul(UT, k);
+        }
+        if (ts < e)
+            walk_add63<true>(ut, 0, target, p, ts - job.n0, e - ts - 1, job.fb);
         uint32_t tlo[BS];
         uint64_t t = target;
 #pragma unroll
@@ -275,10 +316,29 @@ __device__ __forceinline__ void run_doubling(const JobView &job, uint64_t p, uin
             tlo[j] = (uint32_t)t;
             t = half63(t, p);
         }
-        const uint64_t ub = bsgs_blocks<true>(m, u, 0, target, tlo, m.pow2(BS), s - job.n0, nblk, job.fb);
-        const uint64_t done = nblk * BS;  // terms s .. s+done-1 tested
-        if (done < e - s)
-            walk_add63<true>(ub, 0, target, p, s + done - job.n0, e - s - done - 1, job.fb);
+        const uint32_t plo = (uint32_t)p, phi = (uint32_t)(p >> 32), pinv32 = (uint32_t)m.pinv;
+        const uint32_t one = (uint32_t)(p & 1);
+        uint64_t ub = redc32(ut, plo, phi, pinv32, one);  // state at the last block's start
+        const uint64_t idx = s - job.n0;
+        uint64_t left = nblk;
+        while (left) {
+            const uint32_t chunk = left > 0x40000000ull ? 0x40000000u : (uint32_t)left;
+            const uint64_t base = left - chunk;  // blocks base .. left-1 in this chunk
+            for (uint32_t bk = chunk; bk-- > 0;) {
+                if (match16((uint32_t)ub, tlo, 0) | match16((uint32_t)ub, tlo, 16)) {
+                    uint64_t v = ub;
+                    const uint64_t at = idx + (base + bk) * BS;
+#pragma unroll 1
+                    for (int j = 0; j < BS; ++j) {
+                        if (v == target)
+                            push(job.fb, at + j, p);
+                        v = add63(v, v, p);
+                    }
+                }
+                ub = redc32(ub, plo, phi, pinv32, one);
+            }
+            left = base;
+        }
     } else if (p < (1ull << 63))
         walk_add63<true>(u, 0, target, p, s - job.n0, steps, job.fb);
     else
@@ -372,7 +432,11 @@ __device__ __forceinline__ void run_fibonacci(const JobView &job, uint64_t p, ui
     uint64_t i = 0;
     if (p < (1ull << 63)) {
         const uint32_t zero = 0;
-        for (; i + UNROLL <= steps; i += UNROLL) {
+        // blocks of UNROLL steps counted in 32-bit chunks
+        uint64_t nb = steps / UNROLL;
+        while (nb) {
+          const uint32_t chunk = nb > 0x40000000ull ? 0x40000000u : (uint32_t)nb;
+          for (uint32_t bk = 0; bk < chunk; ++bk) {
             const uint64_t a0 = a, b0 = b;
             uint32_t cand;
             // a <- a + b, b <- b + a alternately: (a, b) is (S(n-1), S(n))
@@ -388,15 +452,19 @@ __device__ __forceinline__ void run_fibonacci(const JobView &job, uint64_t p, ui
                 : "l"(p), "r"(zero));
             if (cand) {
                 uint64_t x = a0, y = b0;
+                const uint64_t at = idx + i + (uint64_t)bk * UNROLL;
 #pragma unroll 1
                 for (int j = 0; j < UNROLL; ++j) {
                     uint64_t c = add63(x, y, p);
                     x = y;
                     y = c;
                     if (c == 0)
-                        push(job.fb, idx + i + j + 1, p);
+                        push(job.fb, at + j + 1, p);
                 }
             }
+          }
+          i += (uint64_t)chunk * UNROLL;
+          nb -= chunk;
         }
     }
     for (; i < steps; ++i) {
@@ -483,7 +551,11 @@ __device__ __forceinline__ void run_tribonacci(const JobView &job, uint64_t p, u
         constexpr int TB = 6;
         const uint32_t zero = 0;
         const uint64_t p2 = 2 * p;
-        for (; i + TB <= steps; i += TB) {
+        // blocks of TB steps counted in 32-bit chunks
+        uint64_t nb = steps / TB;
+        while (nb) {
+          const uint32_t chunk = nb > 0x40000000ull ? 0x40000000u : (uint32_t)nb;
+          for (uint32_t bk = 0; bk < chunk; ++bk) {
             const uint64_t x0 = x, y0 = y, z0 = z;
             uint32_t cand;
             asm(CTD_BLOCK_HEAD("%6")
@@ -495,6 +567,7 @@ __device__ __forceinline__ void run_tribonacci(const JobView &job, uint64_t p, u
                 : "l"(p), "l"(p2), "r"(zero));
             if (cand) {
                 uint64_t a = x0, b = y0, c = z0;
+                const uint64_t at = idx + 3 + i + (uint64_t)bk * TB;
 #pragma unroll 1
                 for (int j = 0; j < TB; ++j) {
                     uint64_t w = trib_add(a, b, c, p);
@@ -502,9 +575,12 @@ __device__ __forceinline__ void run_tribonacci(const JobView &job, uint64_t p, u
                     b = c;
                     c = w;
                     if (w == 0)
-                        push(job.fb, idx + 3 + i + j, p);
+                        push(job.fb, at + j, p);
                 }
             }
+          }
+          i += (uint64_t)chunk * TB;
+          nb -= chunk;
         }
     }
     for (; i < steps; ++i) {
