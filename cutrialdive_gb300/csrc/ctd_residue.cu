@@ -702,6 +702,57 @@ __device__ __forceinline__ uint64_t smarandache_walk64(const JobView &job, uint6
     return x;
 }
 
+// Steps m = mm .. mend-1 of x <- x M + m with a Barrett quotient from one
+// 32x32 high multiply: for 2^sh <= p < 2^(sh+1), mu = floor(2^(sh+32) / p)
+// (< 2^32), T = x M + m < 2^(sh+32), q = mulhi(T >> sh, mu) is within 2 of
+// floor(T / p) from below, so x' = T - q p stays in [0, 3p) and
+// x = 0 mod p <=> x in {0, p, 2p}.  T and T - q p are multiply-adds
+// (T - q p = T + q (2^64 - p) mod 2^64).  Needs 3p M + e < 2^64 and
+// 3M + 1 <= 2^31 (checked by the caller).  WIDE: sh >= 32.
+template <bool WIDE>
+__device__ __forceinline__ uint64_t smarandache_walk_b32(const JobView &job, uint64_t p, uint64_t x, uint32_t M,
+                                                         uint32_t sh, uint32_t mu, uint64_t mm, uint64_t mend)
+{
+    const uint64_t np = (uint64_t)0 - p;
+    const uint32_t nplo = (uint32_t)np, nphi = (uint32_t)(np >> 32);
+    const uint32_t plo = (uint32_t)p, p2lo = (uint32_t)(2 * p);
+    auto step = [&](uint64_t v, uint64_t mv) {
+        uint64_t T = (uint64_t)(uint32_t)v * M + mv;
+        T += (uint64_t)((uint32_t)(v >> 32) * M) << 32;
+        const uint32_t top = WIDE ? ((uint32_t)(T >> 32) >> (sh - 32)) : __funnelshift_r((uint32_t)T, (uint32_t)(T >> 32), sh);
+        const uint32_t q = __umulhi(top, mu);
+        uint64_t r = (uint64_t)q * nplo + T;
+        r += (uint64_t)(q * nphi) << 32;
+        return r;
+    };
+    while (mm + UNROLL <= mend) {
+        const uint64_t x0 = x;
+        bool cand = false;
+#pragma unroll
+        for (int j = 0; j < UNROLL; ++j) {
+            x = step(x, mm + j);
+            const uint32_t lo = (uint32_t)x;
+            cand |= (lo == 0u) | (lo == plo) | (lo == p2lo);
+        }
+        if (cand) {
+            uint64_t y = x0;
+#pragma unroll 1
+            for (int j = 0; j < UNROLL; ++j) {
+                y = step(y, mm + j);
+                if (y == 0 || y == p || y == 2 * p)
+                    push(job.fb, (mm + j) - job.n0, p);
+            }
+        }
+        mm += UNROLL;
+    }
+    for (; mm < mend; ++mm) {
+        x = step(x, mm);
+        if (x == 0 || x == p || x == 2 * p)
+            push(job.fb, mm - job.n0, p);
+    }
+    return x;
+}
+
 __device__ __forceinline__ void run_smarandache(const JobView &job, uint64_t p, uint64_t s, uint64_t e)
 {
     const uint64_t b = job.param;
@@ -762,12 +813,26 @@ __device__ __forceinline__ void run_smarandache(const JobView &job, uint64_t p, 
         // words only; a block with a candidate is replayed with the full test.
         uint64_t x = m.from(X);
         const uint32_t plo = (uint32_t)p, p2lo = (uint32_t)(2 * p);
+        // Barrett-32 constants (p < 2^48): sh = floor(log2 p), mu = floor(2^(sh+32) / p)
+        const uint32_t sh = 63 - clz64(p);
+        uint32_t mu = 0;
+        if (p < (1ull << 48)) {
+            const uint64_t mu64 = m.mu();
+            mu = sh <= 32 ? (uint32_t)(mu64 >> (32 - sh))
+                          : (uint32_t)((mu64 << (sh - 32)) + ((m.one << (sh - 32)) / p));
+        }
         while (mcur < e) {
             uint64_t pw;
             const uint64_t cend = class_end(b, mcur, pw);
             const uint64_t mend = cend < e ? cend : e;
             const uint64_t M = pw < p ? pw : pw % p;
-            if (M >> 32)
+            // Barrett-32 when 3pM + e < 2^64 and 3M + 1 <= 2^31 (x < 3p on entry either way)
+            const bool b32 = mu && M < (1ull << 29) && M * 3 + 1 <= (1ull << 31) && p <= (~0ull - e) / (3 * M + 1);
+            if (b32 && sh >= 32)
+                x = smarandache_walk_b32<true>(job, p, x, (uint32_t)M, sh, mu, mcur, mend);
+            else if (b32)
+                x = smarandache_walk_b32<false>(job, p, x, (uint32_t)M, sh, mu, mcur, mend);
+            else if (M >> 32)
                 x = smarandache_walk64<false>(job, p, x, M, m.shoup(M), mcur, mend, plo, p2lo);
             else
                 x = smarandache_walk64<true>(job, p, x, M, m.shoup(M), mcur, mend, plo, p2lo);
