@@ -208,28 +208,30 @@ constexpr int BS = 32;
 // halving mod odd p < 2^63: x/2 or (x + p)/2
 __device__ __forceinline__ uint64_t half63(uint64_t x, uint64_t p) { return (x + ((x & 1) ? p : 0)) >> 1; }
 
-// Nonzero iff lo equals one of t[k .. k+15]: sixteen predicate-accumulating
-// compares in four independent chains (one ALU instruction each).
-__device__ __forceinline__ uint32_t match16(uint32_t lo, const uint32_t (&t)[BS], int k)
+// Nonzero iff lo equals one of the BS = 32 targets t[]: 32 predicate-
+// accumulating compares (one ALU instruction each) in four independent
+// chains, merged into one flag.
+#define CTD_M4(A, B, C, D)                                                                        \
+    "setp.eq.or.u32 c0, %1, %" #A ", c0;\n\tsetp.eq.or.u32 c1, %1, %" #B ", c1;\n\t"           \
+    "setp.eq.or.u32 c2, %1, %" #C ", c2;\n\tsetp.eq.or.u32 c3, %1, %" #D ", c3;\n\t"
+__device__ __forceinline__ uint32_t match32(uint32_t lo, const uint32_t (&t)[BS])
 {
     uint32_t f;
     asm("{\n\t.reg .pred c<4>;\n\t"
         "setp.eq.u32 c0, %1, %2;\n\tsetp.eq.u32 c1, %1, %3;\n\t"
         "setp.eq.u32 c2, %1, %4;\n\tsetp.eq.u32 c3, %1, %5;\n\t"
-        "setp.eq.or.u32 c0, %1, %6, c0;\n\tsetp.eq.or.u32 c1, %1, %7, c1;\n\t"
-        "setp.eq.or.u32 c2, %1, %8, c2;\n\tsetp.eq.or.u32 c3, %1, %9, c3;\n\t"
-        "setp.eq.or.u32 c0, %1, %10, c0;\n\tsetp.eq.or.u32 c1, %1, %11, c1;\n\t"
-        "setp.eq.or.u32 c2, %1, %12, c2;\n\tsetp.eq.or.u32 c3, %1, %13, c3;\n\t"
-        "setp.eq.or.u32 c0, %1, %14, c0;\n\tsetp.eq.or.u32 c1, %1, %15, c1;\n\t"
-        "setp.eq.or.u32 c2, %1, %16, c2;\n\tsetp.eq.or.u32 c3, %1, %17, c3;\n\t"
+        CTD_M4(6, 7, 8, 9) CTD_M4(10, 11, 12, 13) CTD_M4(14, 15, 16, 17) CTD_M4(18, 19, 20, 21)
+        CTD_M4(22, 23, 24, 25) CTD_M4(26, 27, 28, 29) CTD_M4(30, 31, 32, 33)
         "or.pred c0, c0, c1;\n\tor.pred c2, c2, c3;\n\tor.pred c0, c0, c2;\n\t"
         "selp.u32 %0, 1, 0, c0;\n\t}"
         : "=r"(f)
-        : "r"(lo), "r"(t[k]), "r"(t[k + 1]), "r"(t[k + 2]), "r"(t[k + 3]), "r"(t[k + 4]), "r"(t[k + 5]),
-          "r"(t[k + 6]), "r"(t[k + 7]), "r"(t[k + 8]), "r"(t[k + 9]), "r"(t[k + 10]), "r"(t[k + 11]),
-          "r"(t[k + 12]), "r"(t[k + 13]), "r"(t[k + 14]), "r"(t[k + 15]));
+        : "r"(lo), "r"(t[0]), "r"(t[1]), "r"(t[2]), "r"(t[3]), "r"(t[4]), "r"(t[5]), "r"(t[6]), "r"(t[7]),
+          "r"(t[8]), "r"(t[9]), "r"(t[10]), "r"(t[11]), "r"(t[12]), "r"(t[13]), "r"(t[14]), "r"(t[15]),
+          "r"(t[16]), "r"(t[17]), "r"(t[18]), "r"(t[19]), "r"(t[20]), "r"(t[21]), "r"(t[22]), "r"(t[23]),
+          "r"(t[24]), "r"(t[25]), "r"(t[26]), "r"(t[27]), "r"(t[28]), "r"(t[29]), "r"(t[30]), "r"(t[31]));
     return f;
 }
+#undef CTD_M4
 
 // u * 2^-32 mod p for u < p, odd p < 2^63: one 32-bit Montgomery reduction,
 // m = u_lo (-p^-1) mod 2^32, r = (u + m p) / 2^32.  u + m p = 0 mod 2^32 and
@@ -257,7 +259,7 @@ __device__ __forceinline__ uint64_t bsgs_blocks(const Mont &m, uint64_t u, uint6
     const uint64_t p = m.p;
     for (uint64_t b = 0; b < nblk; ++b) {
         const uint32_t lo = (uint32_t)u;
-        if (match16(lo, tlo, 0) | match16(lo, tlo, 16)) {
+        if (match32(lo, tlo)) {
             uint64_t v = u;
 #pragma unroll 1
             for (int j = 0; j < BS; ++j) {
@@ -325,7 +327,7 @@ __device__ __forceinline__ void run_doubling(const JobView &job, uint64_t p, uin
             const uint32_t chunk = left > 0x40000000ull ? 0x40000000u : (uint32_t)left;
             const uint64_t base = left - chunk;  // blocks base .. left-1 in this chunk
             for (uint32_t bk = chunk; bk-- > 0;) {
-                if (match16((uint32_t)ub, tlo, 0) | match16((uint32_t)ub, tlo, 16)) {
+                if (match32((uint32_t)ub, tlo)) {
                     uint64_t v = ub;
                     const uint64_t at = idx + (base + bk) * BS;
 #pragma unroll 1
