@@ -210,7 +210,7 @@ def run_reference(args, world, rank):
     threads = os.cpu_count() or 1
     import oracle  # noqa: F401  (fails loudly if missing)
 
-    per_step_s = 2.0
+    per_step_s = args.cpu_seconds
     total_updates, total_t, samples = 0, 0.0, []
     for i in range(args.warmup + args.steps):
         lo, _ = wl.segment(i)
@@ -649,6 +649,8 @@ def main() -> int:
     ap.add_argument("--shrink", type=int, default=256, help="batched/served: keep the first 1/shrink of each TF range")
     ap.add_argument("--rates", default="1,5,10,25,50", help="served: arrival rates in jobs/s")
     ap.add_argument("--window", type=float, default=10.0, help="served: seconds of arrivals per rate")
+    ap.add_argument("--cpu-seconds", type=float, default=2.0,
+                    help="--impl reference: seconds of CPU work per step (a bounded sample of the step)")
     args = ap.parse_args()
     if not args.steps:
         args.steps = PLAIN[args.workload].default_steps if args.workload in PLAIN else 3
