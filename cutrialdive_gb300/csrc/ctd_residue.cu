@@ -247,32 +247,6 @@ __device__ __forceinline__ uint64_t redc32(uint64_t u, uint32_t plo, uint32_t ph
     return (uint64_t)m * phi + h;
 }
 
-// Tests the terms idx .. idx + nblk*BS - 1 of u -> 2u (DOUBLE) or
-// u -> u + c, starting from state u at idx; returns the state at
-// idx + nblk*BS.  tlo[j] = low word of the j-step target; W = the giant step
-// (Montgomery form of 2^BS for doubling, BS*c mod p for the add).
-template <bool DOUBLE>
-__device__ __forceinline__ uint64_t bsgs_blocks(const Mont &m, uint64_t u, uint64_t c, uint64_t target,
-                                                const uint32_t (&tlo)[BS], uint64_t W, uint64_t idx,
-                                                uint64_t nblk, const FactorsView &fb)
-{
-    const uint64_t p = m.p;
-    for (uint64_t b = 0; b < nblk; ++b) {
-        const uint32_t lo = (uint32_t)u;
-        if (match32(lo, tlo)) {
-            uint64_t v = u;
-#pragma unroll 1
-            for (int j = 0; j < BS; ++j) {
-                if (v == target)
-                    push(fb, idx + b * BS + j, p);
-                v = DOUBLE ? add63(v, v, p) : add63(v, c, p);
-            }
-        }
-        u = DOUBLE ? m.mul(u, W) : add63(u, W, p);
-    }
-    return u;
-}
-
 // ------------------------------------------------------------- families
 
 // Proth k*2^n+1, Riesel k*2^n-1, Mersenne 2^n-1 (riesel_proth.hpp:90-115,
@@ -373,10 +347,30 @@ __device__ __forceinline__ void run_fixed_n(const JobView &job, uint64_t p, uint
 #pragma unroll
         for (int j = 0; j < 5; ++j)  // BS c = 2^5 c
             W = dblmod(W, p);
-        const uint64_t vb = bsgs_blocks<false>(m, v, c, target, tlo, W, s - job.n0, nblk, job.fb);
-        const uint64_t done = nblk * BS;
-        if (done < e - s)
-            walk_add63<false>(vb, c, target, p, s + done - job.n0, e - s - done - 1, job.fb);
+        uint64_t vb = v;
+        uint64_t at0 = s - job.n0;  // index of the current chunk's first term
+        uint64_t left = nblk;
+        while (left) {
+            const uint32_t chunk = left > 0x40000000ull ? 0x40000000u : (uint32_t)left;
+            for (uint32_t bk = 0; bk < chunk; ++bk) {
+                if (match32((uint32_t)vb, tlo)) {
+                    const uint64_t tgt = (FAM == PROTH_FIXED_N) ? p - 1 : 1;
+                    uint64_t x = vb;
+#pragma unroll 1
+                    for (int j = 0; j < BS; ++j) {
+                        if (x == tgt)
+                            push(job.fb, at0 + (uint64_t)bk * BS + j, p);
+                        x = add63(x, c, p);
+                    }
+                }
+                vb = add63(vb, W, p);
+            }
+            at0 += (uint64_t)chunk * BS;
+            left -= chunk;
+        }
+        const uint64_t ts = s + nblk * BS;
+        if (ts < e)
+            walk_add63<false>(vb, c, target, p, ts - job.n0, e - ts - 1, job.fb);
     } else if (p < (1ull << 63))
         walk_add63<false>(v, c, target, p, s - job.n0, steps, job.fb);
     else
@@ -434,12 +428,14 @@ __device__ __forceinline__ void run_fibonacci(const JobView &job, uint64_t p, ui
     uint64_t i = 0;
     if (p < (1ull << 63)) {
         const uint32_t zero = 0;
-        // blocks of UNROLL steps counted in 32-bit chunks
-        uint64_t nb = steps / UNROLL;
+        constexpr int FB = 16;  // steps per block
+        // blocks of FB steps counted in 32-bit chunks; the state at a block's
+        // start is not saved: a block with a candidate steps back FB times
+        // ((S(k-1), S(k)) -> (S(k) - S(k-1), S(k-1))) and replays
+        uint64_t nb = steps / FB;
         while (nb) {
           const uint32_t chunk = nb > 0x40000000ull ? 0x40000000u : (uint32_t)nb;
           for (uint32_t bk = 0; bk < chunk; ++bk) {
-            const uint64_t a0 = a, b0 = b;
             uint32_t cand;
             // a <- a + b, b <- b + a alternately: (a, b) is (S(n-1), S(n))
             // again after every second step, with no register moves
@@ -449,14 +445,24 @@ __device__ __forceinline__ void run_fibonacci(const JobView &job, uint64_t p, ui
                 CTD_ADD_STEP("%0", "%1", "%3", "%4") CTD_ADD_STEP("%1", "%0", "%3", "%4")
                 CTD_ADD_STEP("%0", "%1", "%3", "%4") CTD_ADD_STEP("%1", "%0", "%3", "%4")
                 CTD_ADD_STEP("%0", "%1", "%3", "%4") CTD_ADD_STEP("%1", "%0", "%3", "%4")
+                CTD_ADD_STEP("%0", "%1", "%3", "%4") CTD_ADD_STEP("%1", "%0", "%3", "%4")
+                CTD_ADD_STEP("%0", "%1", "%3", "%4") CTD_ADD_STEP("%1", "%0", "%3", "%4")
+                CTD_ADD_STEP("%0", "%1", "%3", "%4") CTD_ADD_STEP("%1", "%0", "%3", "%4")
+                CTD_ADD_STEP("%0", "%1", "%3", "%4") CTD_ADD_STEP("%1", "%0", "%3", "%4")
                 CTD_BLOCK_TAIL("%2")
                 : "+l"(a), "+l"(b), "=r"(cand)
                 : "l"(p), "r"(zero));
             if (cand) {
-                uint64_t x = a0, y = b0;
-                const uint64_t at = idx + i + (uint64_t)bk * UNROLL;
+                uint64_t x = a, y = b;
 #pragma unroll 1
-                for (int j = 0; j < UNROLL; ++j) {
+                for (int j = 0; j < FB; ++j) {
+                    const uint64_t w = submod(y, x, p);
+                    y = x;
+                    x = w;
+                }
+                const uint64_t at = idx + i + (uint64_t)bk * FB;
+#pragma unroll 1
+                for (int j = 0; j < FB; ++j) {
                     uint64_t c = add63(x, y, p);
                     x = y;
                     y = c;
@@ -465,7 +471,7 @@ __device__ __forceinline__ void run_fibonacci(const JobView &job, uint64_t p, ui
                 }
             }
           }
-          i += (uint64_t)chunk * UNROLL;
+          i += (uint64_t)chunk * FB;
           nb -= chunk;
         }
     }
@@ -550,17 +556,21 @@ __device__ __forceinline__ void run_tribonacci(const JobView &job, uint64_t p, u
     const uint64_t steps = len - 3;  // values T(s+3) .. T(e-1)
     uint64_t i = 0;                   // value T(s+3+i) goes to index idx+3+i
     if (p < (1ull << 62)) {
-        constexpr int TB = 6;
+        constexpr int TB = 12;  // steps per block
         const uint32_t zero = 0;
         const uint64_t p2 = 2 * p;
-        // blocks of TB steps counted in 32-bit chunks
+        // blocks of TB steps counted in 32-bit chunks; a block with a
+        // candidate steps back TB times ((T(k), T(k+1), T(k+2)) ->
+        // (T(k+2) - T(k+1) - T(k), T(k), T(k+1))) and replays
         uint64_t nb = steps / TB;
         while (nb) {
           const uint32_t chunk = nb > 0x40000000ull ? 0x40000000u : (uint32_t)nb;
           for (uint32_t bk = 0; bk < chunk; ++bk) {
-            const uint64_t x0 = x, y0 = y, z0 = z;
             uint32_t cand;
             asm(CTD_BLOCK_HEAD("%6")
+                CTD_TRIB_STEP("%0", "%1", "%2") CTD_TRIB_STEP("%1", "%2", "%0")
+                CTD_TRIB_STEP("%2", "%0", "%1") CTD_TRIB_STEP("%0", "%1", "%2")
+                CTD_TRIB_STEP("%1", "%2", "%0") CTD_TRIB_STEP("%2", "%0", "%1")
                 CTD_TRIB_STEP("%0", "%1", "%2") CTD_TRIB_STEP("%1", "%2", "%0")
                 CTD_TRIB_STEP("%2", "%0", "%1") CTD_TRIB_STEP("%0", "%1", "%2")
                 CTD_TRIB_STEP("%1", "%2", "%0") CTD_TRIB_STEP("%2", "%0", "%1")
@@ -568,7 +578,14 @@ __device__ __forceinline__ void run_tribonacci(const JobView &job, uint64_t p, u
                 : "+l"(x), "+l"(y), "+l"(z), "=r"(cand)
                 : "l"(p), "l"(p2), "r"(zero));
             if (cand) {
-                uint64_t a = x0, b = y0, c = z0;
+                uint64_t a = x, b = y, c = z;
+#pragma unroll 1
+                for (int j = 0; j < TB; ++j) {
+                    const uint64_t w = submod(submod(c, b, p), a, p);
+                    c = b;
+                    b = a;
+                    a = w;
+                }
                 const uint64_t at = idx + 3 + i + (uint64_t)bk * TB;
 #pragma unroll 1
                 for (int j = 0; j < TB; ++j) {
