@@ -744,15 +744,35 @@ __device__ __forceinline__ uint64_t smarandache_walk_b32(const JobView &job, uin
         r += (uint64_t)(q * nphi) << 32;
         return r;
     };
+    // eight steps per PTX block: the multiply-adds (and the counter m) on
+    // the multiply pipe, the shift and the three low-word compares on the ALU.
+    // operands: %0 x, %1 candidate flag, %2 m, %3 M, %4 shift, %5 mu, %6/%7
+    // low/high word of 2^64 - p, %8 low word of p, %9 low word of 2p, %10 one
+#define CTD_SM_STEP(SHIFT)                                                                      \
+    "mov.b64 {xl, xh}, %0;\n\tmad.wide.u32 t, xl, %3, %2;\n\tmov.b64 {tl, th}, t;\n\t"        \
+    "mad.lo.u32 th, xh, %3, th;\n\t" SHIFT "mul.hi.u32 q, top, %5;\n\tmov.b64 t, {tl, th};\n\t"  \
+    "mad.wide.u32 %0, q, %6, t;\n\tmov.b64 {xl, xh}, %0;\n\tmad.lo.u32 xh, q, %7, xh;\n\t"     \
+    "mov.b64 %0, {xl, xh};\n\tsetp.eq.or.u32 c, xl, 0, c;\n\tsetp.eq.or.u32 c, xl, %8, c;\n\t"  \
+    "setp.eq.or.u32 c, xl, %9, c;\n\tmad.wide.u32 %2, %10, %10, %2;\n\t"
+#define CTD_SM_BLOCK(SHIFT)                                                                     \
+    "{\n\t.reg .pred c;\n\t.reg .b32 xl, xh, tl, th, top, q;\n\t.reg .b64 t;\n\t"             \
+    "setp.ne.u32 c, %3, %3;\n\t" CTD_SM_STEP(SHIFT) CTD_SM_STEP(SHIFT) CTD_SM_STEP(SHIFT)          \
+    CTD_SM_STEP(SHIFT) CTD_SM_STEP(SHIFT) CTD_SM_STEP(SHIFT) CTD_SM_STEP(SHIFT) CTD_SM_STEP(SHIFT)  \
+    "selp.u32 %1, 1, 0, c;\n\t}"
+    const uint32_t one = (uint32_t)(p & 1);  // 1 (p is odd), opaque to the compiler
+    const uint32_t shift = WIDE ? sh - 32 : sh;
+    uint64_t mv = mm;
     while (mm + UNROLL <= mend) {
         const uint64_t x0 = x;
-        bool cand = false;
-#pragma unroll
-        for (int j = 0; j < UNROLL; ++j) {
-            x = step(x, mm + j);
-            const uint32_t lo = (uint32_t)x;
-            cand |= (lo == 0u) | (lo == plo) | (lo == p2lo);
-        }
+        uint32_t cand;
+        if (WIDE)
+            asm(CTD_SM_BLOCK("shr.u32 top, th, %4;\n\t")
+                : "+l"(x), "=r"(cand), "+l"(mv)
+                : "r"(M), "r"(shift), "r"(mu), "r"(nplo), "r"(nphi), "r"(plo), "r"(p2lo), "r"(one));
+        else
+            asm(CTD_SM_BLOCK("shf.r.clamp.b32 top, tl, th, %4;\n\t")
+                : "+l"(x), "=r"(cand), "+l"(mv)
+                : "r"(M), "r"(shift), "r"(mu), "r"(nplo), "r"(nphi), "r"(plo), "r"(p2lo), "r"(one));
         if (cand) {
             uint64_t y = x0;
 #pragma unroll 1
@@ -764,6 +784,8 @@ __device__ __forceinline__ uint64_t smarandache_walk_b32(const JobView &job, uin
         }
         mm += UNROLL;
     }
+#undef CTD_SM_BLOCK
+#undef CTD_SM_STEP
     for (; mm < mend; ++mm) {
         x = step(x, mm);
         if (x == 0 || x == p || x == 2 * p)
