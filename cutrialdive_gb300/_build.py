@@ -25,7 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-I", INCLUDE]
 
 CU_SOURCES = ["ctd_residue.cu", "ctd_sieve.cu", "ctd_engine.cu", "ctd_noalloc.cu", "ctd_batch.cu"]
-HEADERS = ["ctd_arith.cuh", "ctd_internal.h"]
+HEADERS = ["ctd_arith.cuh", "ctd_smarandache.cuh", "ctd_internal.h"]
 CLI_SOURCES = ["cli/main.cpp", "cli/command_line.cpp", "cli/results.cpp"]
 
 

@@ -15,6 +15,7 @@
 // Hits are exact: a prime is pushed for index n iff p | S(n), exactly the
 // set the reference's Barrett propagation yields.
 #include "ctd_arith.cuh"
+#include "ctd_smarandache.cuh"
 #include "ctd_internal.h"
 
 #include <atomic>
@@ -258,67 +259,63 @@ __device__ __forceinline__ void run_doubling(const JobView &job, uint64_t p, uin
 {
     Mont m;
     m.init_lite(p);
-    const uint64_t U = m.pow2(s);  // 2^s in Montgomery form
-    uint64_t u;
-    if (FAM == MERSENNE) {
-        u = m.from(U);
-    } else {
-        // Montgomery form times a plain k leaves the plain k*2^s mod p
-        const uint64_t k = job.param < p ? job.param : job.param % p;
-        u = m.mul(U, k);
-    }
     const uint64_t target = (FAM == PROTH) ? p - 1 : 1;
     const uint64_t steps = e - s - 1;
     const uint64_t nblk = (e - s) / BS;
+    // u(s) = k 2^s mod p, for the per-step walks
+    auto start = [&]() {
+        const uint64_t U = m.pow2(s);  // 2^s in Montgomery form
+        if (FAM == MERSENNE)
+            return m.from(U);
+        // Montgomery form times a plain k leaves the plain k*2^s mod p
+        const uint64_t k = job.param < p ? job.param : job.param % p;
+        return m.mul(U, k);
+    };
     if (p < (1ull << 63) && nblk >= 2) {
-        // blocks walked backwards: the giant step u -> u 2^-32 is one
-        // reduction on the multiply pipe (redc32).  Start from the state at
-        // the end of the last whole block, walk the short tail forwards.
-        const uint64_t ts = s + nblk * BS;
-        const uint64_t UT = m.pow2(ts);
-        uint64_t ut;
-        if (FAM == MERSENNE) {
-            ut = m.from(UT);
-        } else {
-            const uint64_t k = job.param < p ? job.param : job.param % p;
-            ut = m.mul(UT, k);
-        }
-        if (ts < e)
-            walk_add63<true>(ut, 0, target, p, ts - job.n0, e - ts - 1, job.fb);
+        // Walk w(n) = 2^-n instead: k 2^n = -1 (Proth) / 1 (Riesel, Mersenne
+        // with k = 1) mod p iff w(n) = -k / k, a fixed target, and the giant
+        // step w -> w 2^-32 is one reduction on the multiply pipe (redc32).
+        // Term n + j of a block starting at n is a zero iff w(n) = target 2^j.
+        const uint64_t k = FAM == MERSENNE ? 1 : (job.param < p ? job.param : job.param % p);
+        const uint64_t wt = (FAM == PROTH) ? (k ? p - k : 0) : k;  // target of w
+        const uint64_t sr = s < p - 1 ? s : s % (p - 1);
+        uint64_t w = m.from(m.pow2(p - 1 - sr));  // 2^-s mod p (Fermat)
         uint32_t tlo[BS];
-        uint64_t t = target;
+        uint64_t t = wt;
 #pragma unroll
         for (int j = 0; j < BS; ++j) {
             tlo[j] = (uint32_t)t;
-            t = half63(t, p);
+            t = add63(t, t, p);
         }
         const uint32_t plo = (uint32_t)p, phi = (uint32_t)(p >> 32), pinv32 = (uint32_t)m.pinv;
         const uint32_t one = (uint32_t)(p & 1);
-        uint64_t ub = redc32(ut, plo, phi, pinv32, one);  // state at the last block's start
-        const uint64_t idx = s - job.n0;
+        uint64_t at0 = s - job.n0;  // index of the current chunk's first term
         uint64_t left = nblk;
         while (left) {
             const uint32_t chunk = left > 0x40000000ull ? 0x40000000u : (uint32_t)left;
-            const uint64_t base = left - chunk;  // blocks base .. left-1 in this chunk
-            for (uint32_t bk = chunk; bk-- > 0;) {
-                if (match32((uint32_t)ub, tlo)) {
-                    uint64_t v = ub;
-                    const uint64_t at = idx + (base + bk) * BS;
+            for (uint32_t bk = 0; bk < chunk; ++bk) {
+                if (match32((uint32_t)w, tlo)) {
+                    uint64_t v = w;
 #pragma unroll 1
                     for (int j = 0; j < BS; ++j) {
-                        if (v == target)
-                            push(job.fb, at + j, p);
-                        v = add63(v, v, p);
+                        if (v == wt)
+                            push(job.fb, at0 + (uint64_t)bk * BS + j, p);
+                        v = half63(v, p);
                     }
                 }
-                ub = redc32(ub, plo, phi, pinv32, one);
+                w = redc32(w, plo, phi, pinv32, one);
             }
-            left = base;
+            at0 += (uint64_t)chunk * BS;
+            left -= chunk;
         }
-    } else if (p < (1ull << 63))
-        walk_add63<true>(u, 0, target, p, s - job.n0, steps, job.fb);
+        for (uint64_t n = s + nblk * BS; n < e; ++n) {  // the short tail, term by term
+            if (w == wt)
+                push(job.fb, n - job.n0, p);
+            w = half63(w, p);
+        }    } else if (p < (1ull << 63))
+        walk_add63<true>(start(), 0, target, p, s - job.n0, steps, job.fb);
     else
-        walk_target(u, target, p, s - job.n0, steps, job.fb, [p](uint64_t x) { return dblmod(x, p); });
+        walk_target(start(), target, p, s - job.n0, steps, job.fb, [p](uint64_t x) { return dblmod(x, p); });
 }
 
 // k*2^n +- 1 with fixed n over the index k (riesel_proth_fixed_n.hpp:88-151):
@@ -613,74 +610,8 @@ __device__ __forceinline__ void run_tribonacci(const JobView &job, uint64_t p, u
 }
 
 // ----------------------------------------------------------- Smarandache
-// Sm_b(n) = Sm_b(n-1) * b^len(n) + n (smarandache.hpp:131-198).  Within a
-// digit class (all m = n+1 with the same length d) the step is the affine
-// map x -> M x + m with M = b^d, so t steps from (x, m = c0) give
-//   x_t = M^t x + c0 G(t) + H(t),  G(t) = sum_{j<t} M^j,  H(t) = sum_{i<t} i M^(t-1-i)
-// with G(2t) = G(t)(1 + M^t), H(2t) = M^t H(t) + t G(t) + H(t),
-//      G(t+1) = M G(t) + 1,     H(t+1) = M H(t) + t.
-// This jump replaces the reference's reduction of the multi-limb Sm_b(n0)
-// (src/trial_factoring.cuh:197-202) and costs O(log n) per digit class.
-
-// smallest power of b above m (the end of m's digit class), saturating
-__device__ __forceinline__ uint64_t class_end(uint64_t b, uint64_t m, uint64_t &pw)
-{
-    pw = b;
-    while (pw <= m) {
-        if (pw > ~0ull / b) {
-            pw = ~0ull;
-            return pw;
-        }
-        pw *= b;
-    }
-    return pw;
-}
-
-// X (Montgomery form) -> after the steps m = c0 .. c0+t-1 with multiplier Mm
-// (Montgomery form).  Left-to-right over the bits of t, keeping (M^k, G(k),
-// H(k), k) for the prefix k read so far; k itself is kept in Montgomery form
-// (K) and updated by doubling and adding one, so no conversion is needed.
-__device__ __forceinline__ uint64_t affine_jump(const Mont &m, uint64_t X, uint64_t Mm, uint64_t c0, uint64_t t)
-{
-    if (!t)
-        return X;
-    uint64_t Mt = m.one, G = 0, H = 0, K = 0;
-    bool started = false;
-    for (int bit = 63 - __clzll(t); bit >= 0; --bit) {
-        if (started) {  // k -> 2k
-            const uint64_t H2 = m.add(m.add(m.mul(Mt, H), m.mul(K, G)), H);
-            G = m.mul(G, m.add(m.one, Mt));
-            Mt = m.mul(Mt, Mt);
-            H = H2;
-            K = m.dbl(K);
-        }
-        if ((t >> bit) & 1) {  // k -> k + 1
-            H = m.add(m.mul(Mm, H), K);
-            G = m.add(m.mul(Mm, G), m.one);
-            Mt = m.mul(Mm, Mt);
-            K = m.add(K, m.one);
-            started = true;
-        }
-    }
-    return m.add(m.add(m.mul(Mt, X), m.mul(m.to(c0), G)), H);
-}
-
-// Sm_b(s) mod p in Montgomery form, from Sm_b(0) = 0 class by class.
-__device__ __forceinline__ uint64_t smarandache_at(const Mont &m, uint64_t b, uint64_t s)
-{
-    uint64_t X = 0;
-    uint64_t c = 1;  // next m to apply
-    while (c <= s) {
-        uint64_t pw;
-        uint64_t cend = class_end(b, c, pw);  // M = pw for m in [c, cend)
-        uint64_t last = cend - 1 < s ? cend - 1 : s;
-        X = affine_jump(m, X, m.to(pw), c, last - c + 1);
-        c = last + 1;
-        if (cend == ~0ull)
-            break;
-    }
-    return X;
-}
+// The jump to Sm_b(s) mod p (class_end, affine_jump, smarandache_at) lives in
+// ctd_smarandache.cuh; the walks below step within one digit class.
 
 // Steps m = mm .. mend-1 of x <- x M + m (x in [1, 3p), M < p, Ms its Shoup
 // quotient); SMALL: M < 2^32.  Returns the final x.
@@ -744,35 +675,15 @@ __device__ __forceinline__ uint64_t smarandache_walk_b32(const JobView &job, uin
         r += (uint64_t)(q * nphi) << 32;
         return r;
     };
-    // eight steps per PTX block: the multiply-adds (and the counter m) on
-    // the multiply pipe, the shift and the three low-word compares on the ALU.
-    // operands: %0 x, %1 candidate flag, %2 m, %3 M, %4 shift, %5 mu, %6/%7
-    // low/high word of 2^64 - p, %8 low word of p, %9 low word of 2p, %10 one
-#define CTD_SM_STEP(SHIFT)                                                                      \
-    "mov.b64 {xl, xh}, %0;\n\tmad.wide.u32 t, xl, %3, %2;\n\tmov.b64 {tl, th}, t;\n\t"        \
-    "mad.lo.u32 th, xh, %3, th;\n\t" SHIFT "mul.hi.u32 q, top, %5;\n\tmov.b64 t, {tl, th};\n\t"  \
-    "mad.wide.u32 %0, q, %6, t;\n\tmov.b64 {xl, xh}, %0;\n\tmad.lo.u32 xh, q, %7, xh;\n\t"     \
-    "mov.b64 %0, {xl, xh};\n\tsetp.eq.or.u32 c, xl, 0, c;\n\tsetp.eq.or.u32 c, xl, %8, c;\n\t"  \
-    "setp.eq.or.u32 c, xl, %9, c;\n\tmad.wide.u32 %2, %10, %10, %2;\n\t"
-#define CTD_SM_BLOCK(SHIFT)                                                                     \
-    "{\n\t.reg .pred c;\n\t.reg .b32 xl, xh, tl, th, top, q;\n\t.reg .b64 t;\n\t"             \
-    "setp.ne.u32 c, %3, %3;\n\t" CTD_SM_STEP(SHIFT) CTD_SM_STEP(SHIFT) CTD_SM_STEP(SHIFT)          \
-    CTD_SM_STEP(SHIFT) CTD_SM_STEP(SHIFT) CTD_SM_STEP(SHIFT) CTD_SM_STEP(SHIFT) CTD_SM_STEP(SHIFT)  \
-    "selp.u32 %1, 1, 0, c;\n\t}"
-    const uint32_t one = (uint32_t)(p & 1);  // 1 (p is odd), opaque to the compiler
-    const uint32_t shift = WIDE ? sh - 32 : sh;
-    uint64_t mv = mm;
     while (mm + UNROLL <= mend) {
         const uint64_t x0 = x;
-        uint32_t cand;
-        if (WIDE)
-            asm(CTD_SM_BLOCK("shr.u32 top, th, %4;\n\t")
-                : "+l"(x), "=r"(cand), "+l"(mv)
-                : "r"(M), "r"(shift), "r"(mu), "r"(nplo), "r"(nphi), "r"(plo), "r"(p2lo), "r"(one));
-        else
-            asm(CTD_SM_BLOCK("shf.r.clamp.b32 top, tl, th, %4;\n\t")
-                : "+l"(x), "=r"(cand), "+l"(mv)
-                : "r"(M), "r"(shift), "r"(mu), "r"(nplo), "r"(nphi), "r"(plo), "r"(p2lo), "r"(one));
+        bool cand = false;
+#pragma unroll
+        for (int j = 0; j < UNROLL; ++j) {
+            x = step(x, mm + j);
+            const uint32_t lo = (uint32_t)x;
+            cand |= (lo == 0u) | (lo == plo) | (lo == p2lo);
+        }
         if (cand) {
             uint64_t y = x0;
 #pragma unroll 1
@@ -784,8 +695,6 @@ __device__ __forceinline__ uint64_t smarandache_walk_b32(const JobView &job, uin
         }
         mm += UNROLL;
     }
-#undef CTD_SM_BLOCK
-#undef CTD_SM_STEP
     for (; mm < mend; ++mm) {
         x = step(x, mm);
         if (x == 0 || x == p || x == 2 * p)
@@ -812,7 +721,7 @@ __device__ __forceinline__ void run_smarandache(const JobView &job, uint64_t p, 
         while (mcur < e) {
             uint64_t pw;
             uint64_t cend = class_end(b, mcur, pw);
-            const uint32_t M = (uint32_t)(pw % p);
+            const uint32_t M = (uint32_t)class_multiplier(m, b, mcur, pw);
             const uint32_t Ms = shoup_precompute32(M, p32);
             uint32_t mm = (uint32_t)mcur;
             const uint32_t mend = (uint32_t)(cend < e ? cend : e);
@@ -866,7 +775,7 @@ __device__ __forceinline__ void run_smarandache(const JobView &job, uint64_t p, 
             uint64_t pw;
             const uint64_t cend = class_end(b, mcur, pw);
             const uint64_t mend = cend < e ? cend : e;
-            const uint64_t M = pw < p ? pw : pw % p;
+            const uint64_t M = class_multiplier(m, b, mcur, pw);
             // Barrett-32 when 3pM + e < 2^64 and 3M + 1 <= 2^31 (x < 3p on entry either way)
             const bool b32 = mu && M < (1ull << 29) && M * 3 + 1 <= (1ull << 31) && p <= (~0ull - e) / (3 * M + 1);
             if (b32 && sh >= 32)
@@ -887,7 +796,7 @@ __device__ __forceinline__ void run_smarandache(const JobView &job, uint64_t p, 
     while (mcur < e) {
         uint64_t pw;
         uint64_t cend = class_end(b, mcur, pw);
-        const uint64_t Mm = m.to(pw);
+        const uint64_t Mm = m.to(class_multiplier(m, b, mcur, pw));
         const uint64_t mend = cend < e ? cend : e;
         for (; mcur < mend; ++mcur) {
             X = m.add(m.mul(X, Mm), C);

@@ -2,7 +2,8 @@
 from the same source and checked against Python integers: Montgomery set-up
 (R mod p, R^2 mod p), 2^e by squaring and doubling, the mixed
 Montgomery-times-plain product that yields k*2^e mod p, and the
-division-free floor(2^64/p) and Shoup quotients floor(w 2^64/p)."""
+division-free floor(2^64/p) and Shoup quotients floor(w 2^64/p); and the
+Smarandache jump to Sm_b(s) mod p (ctd_smarandache.cuh)."""
 import os
 import random
 import shutil
@@ -50,3 +51,45 @@ def test_montgomery_setup_and_pow2(checker):
         assert tok == k % p, (p, k)
         assert mu == R // p, p
         assert sh == (k % p) * R // p, (p, k)
+
+
+def smarandache_mod(b: int, s: int, p: int) -> int:
+    """Sm_b(s) mod p by the definition: concatenate 1 .. s in base b."""
+    x, pw = 0, b
+    for m in range(1, s + 1):
+        while pw <= m:
+            pw *= b
+        x = (x * pw + m) % p
+    return x
+
+
+@pytest.fixture(scope="module")
+def sm_checker(tmp_path_factory):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    exe = str(tmp_path_factory.mktemp("smjump") / "smarandache_host_check")
+    subprocess.check_call([nvcc, "-O2", "-std=c++17", "-o", exe, os.path.join(HERE, "smarandache_host_check.cu")])
+    return exe
+
+
+def test_smarandache_jump_closed_form_and_doubling(sm_checker):
+    """The kernel's jump to Sm_b(s) mod p: closed-form class jumps with one
+    simultaneous inversion, and the doubling jumps, both against Python."""
+    from sympy import prevprime, randprime
+
+    rnd = random.Random(9)
+    cases = [(3, 10, 1), (5, 2, 0), (7, 10, 9), (11, 10, 10), (13, 10, 100), (101, 2, 1000),
+             # p | b^d - 1 (a class multiplier = 1 mod p): 3 | 10 - 1, 7 | 2^3 - 1, 11 | 10^2 - 1
+             (3, 10, 50), (7, 2, 300), (11, 10, 1200), (9901, 10, 5000),
+             (prevprime(1 << 62), 16, 3000), (prevprime(1 << 64), 10, 2000), (prevprime(1 << 30), 2, 40000)]
+    for _ in range(40):
+        p = randprime(3, 1 << rnd.choice([8, 20, 31, 34, 40, 48]))
+        cases.append((p, rnd.randrange(2, 65), rnd.randrange(0, 3000)))
+    inp = "".join(f"{p} {b} {s}\n" for p, b, s in cases)
+    out = subprocess.run([sm_checker], input=inp, capture_output=True, text=True, check=True).stdout.split("\n")
+    for (p, b, s), line in zip(cases, out):
+        closed, dbl = map(int, line.split())
+        want = smarandache_mod(b, s, p)
+        assert closed == want, (p, b, s)
+        assert dbl == want, (p, b, s)
