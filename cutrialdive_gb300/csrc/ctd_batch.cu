@@ -48,11 +48,13 @@ uint64_t job_bytes(const ctd_job &j)
     return counts_bytes(j) + (j.n1 - j.n0) * (uint64_t)j.max_factors * sizeof(uint64_t);
 }
 
-JobView view_of(const ctd_job &j, uint32_t *counts, uint64_t *factors)
+JobView view_of(ctd_ctx *ctx, const ctd_job &j, uint32_t *counts, uint64_t *factors)
 {
     JobView v{};
     v.family = j.family;
     v.tiles = 1;
+    ctd_tuning t{};
+    v.variant = ctd_get_tuning(ctx, j.family, &t) == CTD_OK ? t.variant : CTD_VARIANT_AUTO;
     v.param = j.param;
     v.n0 = j.n0;
     v.n1 = j.n1;
@@ -178,7 +180,7 @@ int ctd_batch_run(ctd_ctx *ctx, const ctd_job *jobs, uint32_t njobs, uint32_t *c
         BATCH_TRY(cudaMemcpyAsync(dc, counts_inout[i], N * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
         BATCH_TRY(cudaMemcpyAsync(df, factors_inout[i], N * j.max_factors * sizeof(uint64_t),
                                   cudaMemcpyHostToDevice, st));
-        hjobs[i].view = view_of(j, dc, df);
+        hjobs[i].view = view_of(ctx, j, dc, df);
         hjobs[i].f0 = odd_f0(j);
         hjobs[i].f1 = j.f1;
         if (j.f0 <= 2 && j.f1 > 2) {  // the prime 2 for this job
@@ -209,6 +211,10 @@ int ctd_batch_run(ctd_ctx *ctx, const ctd_job *jobs, uint32_t njobs, uint32_t *c
             if (byfam.empty())
                 continue;
             for (auto &kv : byfam) {
+                // longest index range first (the kernel hands out items in this order)
+                std::stable_sort(kv.second.begin(), kv.second.end(), [&](uint32_t x, uint32_t y) {
+                    return jobs[x].n1 - jobs[x].n0 > jobs[y].n1 - jobs[y].n0;
+                });
                 for (size_t b = 0; b < kv.second.size(); b += MAX_ACTIVE_PER_LAUNCH) {
                     Launch l;
                     l.family = kv.first;
@@ -367,7 +373,7 @@ int ctd_serve_tick(ctd_server *srv, uint64_t *done_ids, uint32_t cap, uint32_t *
         CTX_TRY(cudaMallocAsync(&q.d_factors, N * q.job.max_factors * sizeof(uint64_t), st));
         CTX_TRY(cudaMemsetAsync(q.d_counts, 0, N * sizeof(uint32_t), st));
         if (q.job.f0 <= 2 && q.job.f1 > 2) {
-            int rc = launch_mod2(view_of(q.job, q.d_counts, q.d_factors), st, err);
+            int rc = launch_mod2(view_of(ctx, q.job, q.d_counts, q.d_factors), st, err);
             if (rc)
                 return ctx_fail(ctx, rc, err);
         }
@@ -404,7 +410,7 @@ int ctd_serve_tick(ctd_server *srv, uint64_t *done_ids, uint32_t cap, uint32_t *
     std::vector<BatchJob> hj(na);
     for (uint32_t i = 0; i < na; ++i) {
         auto &j = srv->active[i];
-        hj[i].view = view_of(j.job, j.d_counts, j.d_factors);
+        hj[i].view = view_of(ctx, j.job, j.d_counts, j.d_factors);
         hj[i].f0 = odd_f0(j.job);
         hj[i].f1 = j.job.f1;
     }
@@ -443,6 +449,11 @@ int ctd_serve_tick(ctd_server *srv, uint64_t *done_ids, uint32_t cap, uint32_t *
             byfam[j.job.family].push_back(i);
         }
         for (auto &f : byfam) {
+            // longest index range first (the kernel hands out items in this order)
+            std::stable_sort(f.second.begin(), f.second.end(), [&](uint32_t x, uint32_t y) {
+                const ctd_job &a = srv->active[x].job, &c = srv->active[y].job;
+                return a.n1 - a.n0 > c.n1 - c.n0;
+            });
             launches.push_back({lo, hi, f.first, (uint32_t)order.size(), (uint32_t)f.second.size()});
             order.insert(order.end(), f.second.begin(), f.second.end());
         }

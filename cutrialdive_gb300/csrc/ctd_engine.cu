@@ -180,6 +180,12 @@ void choose_tiles(const ctd_ctx *ctx, uint32_t family, uint64_t nprimes, uint64_
               t && t->min_tile ? t->min_tile : DEFAULT_MIN_TILE, tiles, tile_len);
 }
 
+uint32_t variant_of(const ctd_ctx *ctx, uint32_t family)
+{
+    const ctd_tuning *t = tuning_of(ctx, family);
+    return t ? t->variant : CTD_VARIANT_AUTO;
+}
+
 uint64_t default_segment(const ctd_ctx *ctx, uint32_t family)
 {
     const ctd_tuning *t = tuning_of(ctx, family);
@@ -335,10 +341,11 @@ int ctd_set_tuning(ctd_ctx *ctx, uint32_t family, const ctd_tuning *t)
         return CTD_OK;
     }
     if (t->block_size < 32 || t->block_size > 256 || (t->block_size % 32) || t->ctas_per_sm < 0 ||
-        t->items_per_thread == 0 || t->min_tile == 0 || (t->segment_log2 && (t->segment_log2 < 20 || t->segment_log2 > 40)))
+        t->items_per_thread == 0 || t->min_tile == 0 || (t->segment_log2 && (t->segment_log2 < 20 || t->segment_log2 > 40)) ||
+        t->variant > CTD_VARIANT_MONTGOMERY)
         return fail(ctx, CTD_ERR_INVALID_ARGUMENT,
                     "ctd_set_tuning: block_size 32..256 (multiple of 32), ctas_per_sm >= 0, items_per_thread and "
-                    "min_tile > 0, segment_log2 0 or 20..40");
+                    "min_tile > 0, segment_log2 0 or 20..40, variant 0..2");
     ctx->tuning[k] = *t;
     ctx->tuned[k] = true;
     return CTD_OK;
@@ -388,6 +395,7 @@ int ctd_autotune(ctd_ctx *ctx, const ctd_job *job, double budget_s, ctd_tuning *
     auto time_config = [&](const ctd_tuning &c, uint64_t n, float &ms) -> int {
         const int grid = grid_for(ctx, job->family, c.block_size, c.ctas_per_sm);
         tiles_for(n, N, grid, c.block_size, c.items_per_thread, c.min_tile, view.tiles, view.tile_len);
+        view.variant = c.variant;
         ms = 1e30f;
         for (int r = 0; r < 3; ++r) {
             if (cudaMemsetAsync(ctx->d_counts, 0, N * sizeof(uint32_t), st) != cudaSuccess)
@@ -409,6 +417,7 @@ int ctd_autotune(ctd_ctx *ctx, const ctd_job *job, double budget_s, ctd_tuning *
     ctd_tuning base = cur;
     base.block_size = 256;
     base.ctas_per_sm = 0;
+    base.variant = CTD_VARIANT_AUTO;
     float best_ms = 0;
     rc = time_config(base, np, best_ms);
     // keep one trial near a sixth of the budget: a prefix of the sample primes
@@ -473,6 +482,23 @@ int ctd_autotune(ctd_ctx *ctx, const ctd_job *job, double budget_s, ctd_tuning *
                 winner = t;
             }
         }
+    // step form: the term-by-term walk against the blocks (doubling, fixed-n),
+    // and the Smarandache step variants
+    const uint32_t fam = job->family;
+    const bool has_walk = fam == CTD_PROTH || fam == CTD_RIESEL || fam == CTD_MERSENNE ||
+                          fam == CTD_PROTH_FIXED_N || fam == CTD_RIESEL_FIXED_N || fam == CTD_SMARANDACHE;
+    for (uint32_t v = CTD_VARIANT_WALK; !rc && has_walk && v <= CTD_VARIANT_MONTGOMERY && elapsed() < budget_s; ++v) {
+        if (v == CTD_VARIANT_MONTGOMERY && fam != CTD_SMARANDACHE)
+            break;
+        ctd_tuning t = winner;
+        t.variant = v;
+        float ms = 0;
+        rc = time_config(t, np, ms);
+        if (!rc && ms < best_ms) {
+            best_ms = ms;
+            winner = t;
+        }
+    }
     cudaEventDestroy(ea);
     cudaEventDestroy(eb);
     if (rc)
@@ -531,6 +557,7 @@ int ctd_residues_device(ctd_ctx *ctx, const ctd_job *job, const uint64_t *d_prim
     CTX_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
     JobView v = make_view(job, d_counts, d_factors);
+    v.variant = variant_of(ctx, job->family);
     const int block = default_block(ctx, job->family);
     const int grid = default_grid(ctx, job->family, block);
     choose_tiles(ctx, job->family, nprimes, job->n1 - job->n0, grid, block, v.tiles, v.tile_len);
@@ -575,6 +602,7 @@ int ctd_run_plain(ctd_ctx *ctx, const ctd_job *job, uint32_t *counts_inout, uint
     CTX_CUDA(cudaMemcpyAsync(ctx->d_counts, counts_inout, N * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
     CTX_CUDA(cudaMemcpyAsync(ctx->d_factors, factors_inout, NF * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
     JobView view = make_view(job, ctx->d_counts, ctx->d_factors);
+    view.variant = variant_of(ctx, job->family);
     std::string err;
 
     uint64_t f0 = resume_after_prime ? resume_after_prime + 1 : job->f0;

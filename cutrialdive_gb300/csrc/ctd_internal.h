@@ -41,6 +41,7 @@ struct FactorsView {
 struct JobView {
     uint32_t family;
     uint32_t tiles;      // index tiles per prime (>= 1)
+    uint32_t variant;    // step form (CTD_VARIANT_*)
     uint64_t param;      // k, n or base
     uint64_t n0, n1;     // index range of the factors buffer
     uint64_t tile_len;   // indices per tile (last tile may be shorter)

@@ -271,7 +271,7 @@ __device__ __forceinline__ void run_doubling(const JobView &job, uint64_t p, uin
         const uint64_t k = job.param < p ? job.param : job.param % p;
         return m.mul(U, k);
     };
-    if (p < (1ull << 63) && nblk >= 2) {
+    if (p < (1ull << 63) && nblk >= 2 && job.variant != CTD_VARIANT_WALK) {
         // Walk w(n) = 2^-n instead: k 2^n = -1 (Proth) / 1 (Riesel, Mersenne
         // with k = 1) mod p iff w(n) = -k / k, a fixed target, and the giant
         // step w -> w 2^-32 is one reduction on the multiply pipe (redc32).
@@ -332,7 +332,7 @@ __device__ __forceinline__ void run_fixed_n(const JobView &job, uint64_t p, uint
     const uint64_t target = (FAM == PROTH_FIXED_N) ? p - 1 : 1;
     const uint64_t steps = e - s - 1;
     const uint64_t nblk = (e - s) / BS;
-    if (p < (1ull << 63) && nblk >= 2) {
+    if (p < (1ull << 63) && nblk >= 2 && job.variant != CTD_VARIANT_WALK) {
         uint32_t tlo[BS];
         uint64_t t = target, W = c;
         const uint64_t nc = p - c == p ? 0 : p - c;  // -c mod p
@@ -713,7 +713,7 @@ __device__ __forceinline__ void run_smarandache(const JobView &job, uint64_t p, 
     if (X == 0)
         push(job.fb, idx0, p);
     uint64_t mcur = s + 1;  // m = n + 1 of the next step
-    if (p < (1u << 30) && p >= e && e <= 0xffffffffull) {
+    if (p < (1u << 30) && p >= e && e <= 0xffffffffull && job.variant != CTD_VARIANT_MONTGOMERY) {
         // 32-bit Shoup path: x kept in [0, 3p) (Shoup output < 2p, plus m < p),
         // so x = 0 mod p <=> x == p or x == 2p (x >= 1 after a step).
         const uint32_t p32 = (uint32_t)p, p2 = 2 * p32;
@@ -756,7 +756,7 @@ __device__ __forceinline__ void run_smarandache(const JobView &job, uint64_t p, 
         }
         return;
     }
-    if (p < (1ull << 62) && e <= p) {
+    if (p < (1ull << 62) && e <= p && job.variant != CTD_VARIANT_MONTGOMERY) {
         // 64-bit Shoup path (every m < p): x kept in [1, 3p) as r + m with
         // r = x M - q p in [0, 2p), q = mulhi(x, floor(M 2^64 / p)); so
         // x = 0 mod p <=> x == p or x == 2p.  The unrolled body tests the low
@@ -766,7 +766,7 @@ __device__ __forceinline__ void run_smarandache(const JobView &job, uint64_t p, 
         // Barrett-32 constants (p < 2^48): sh = floor(log2 p), mu = floor(2^(sh+32) / p)
         const uint32_t sh = 63 - clz64(p);
         uint32_t mu = 0;
-        if (p < (1ull << 48)) {
+        if (p < (1ull << 48) && job.variant == CTD_VARIANT_AUTO) {
             const uint64_t mu64 = m.mu();
             mu = sh <= 32 ? (uint32_t)(mu64 >> (32 - sh))
                           : (uint32_t)((mu64 << (sh - 32)) + ((m.one << (sh - 32)) / p));
@@ -914,35 +914,50 @@ __global__ void __launch_bounds__(1024) batch_bounds_kernel(const BatchJob *__re
             run += spans[i].items;
         }
         spans[nactive].prefix = run;  // total items
+        spans[nactive].items = 0;     // the batch kernel's work counter
     }
 }
 
+// Persistent grid over a device work queue: each warp takes the next 32
+// items (one prime of one job each) from a counter the bounds kernel reset;
+// the host orders a launch's jobs longest index range first, so the long
+// items start early and the short ones fill in at the end.
 template <uint32_t FAM>
 __global__ void __launch_bounds__(256, min_ctas_per_sm(FAM))
 batch_kernel(const BatchJob *__restrict__ jobs, const uint32_t *__restrict__ active, uint32_t nactive,
-             const uint64_t *__restrict__ primes, const BatchSpan *__restrict__ spans)
+             const uint64_t *__restrict__ primes, BatchSpan *__restrict__ spans)
 {
     const uint64_t total = spans[nactive].prefix;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += stride) {
-        // the active job holding item k: last prefix <= k
-        uint32_t lo = 0, hi = nactive;
-        while (hi - lo > 1) {
-            uint32_t mid = (lo + hi) >> 1;
-            if (spans[mid].prefix <= k)
-                lo = mid;
-            else
-                hi = mid;
+    unsigned long long *next = reinterpret_cast<unsigned long long *>(&spans[nactive].items);
+    const uint32_t lane = threadIdx.x & 31u;
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0)
+            base = atomicAdd(next, 32ull);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= total)
+            break;
+        const uint64_t k = base + lane;
+        if (k < total) {
+            // the active job holding item k: last prefix <= k
+            uint32_t lo = 0, hi = nactive;
+            while (hi - lo > 1) {
+                uint32_t mid = (lo + hi) >> 1;
+                if (spans[mid].prefix <= k)
+                    lo = mid;
+                else
+                    hi = mid;
+            }
+            const JobView &v = jobs[active[lo]].view;
+            const uint64_t p = primes[spans[lo].pbeg + (k - spans[lo].prefix)];
+            run_item<FAM>(v, p, v.n0, v.n1);
         }
-        const BatchJob &j = jobs[active[lo]];
-        const uint64_t p = primes[spans[lo].pbeg + (k - spans[lo].prefix)];
-        run_item<FAM>(j.view, p, j.view.n0, j.view.n1);
     }
 }
 
 template <uint32_t FAM>
 static cudaError_t launch_batch_fam(const BatchJob *jobs, const uint32_t *active, uint32_t nactive,
-                                    const uint64_t *primes, const BatchSpan *spans, int grid, cudaStream_t st)
+                                    const uint64_t *primes, BatchSpan *spans, int grid, cudaStream_t st)
 {
     batch_kernel<FAM><<<grid, 256, 0, st>>>(jobs, active, nactive, primes, spans);
     return cudaGetLastError();

@@ -107,9 +107,9 @@ CTD_HD uint64_t smarandache_at_doubling(const Mont &m, uint64_t b, uint64_t s)
 
 constexpr int SM_MAX_CLASSES = 24;
 
-// Sm_b(s) mod p in Montgomery form (needs m.r2; p prime, for the Fermat
-// inversion).
-CTD_HD uint64_t smarandache_at(const Mont &m, uint64_t b, uint64_t s)
+// Sm_b(s) mod p in Montgomery form by the closed-form class jumps (needs
+// m.r2; p prime, for the Fermat inversion).
+CTD_HD uint64_t smarandache_at_closed(const Mont &m, uint64_t b, uint64_t s)
 {
     // the digit classes of 1 .. s: [lo_d, hi_d], multiplier Md (Montgomery form)
     uint64_t Mt[SM_MAX_CLASSES];   // M_d
@@ -158,6 +158,31 @@ CTD_HD uint64_t smarandache_at(const Mont &m, uint64_t b, uint64_t s)
         c = last + 1;
     }
     return X;
+}
+
+// Sm_b(s) mod p in Montgomery form: the cheaper composition by a
+// multiplication count.  The doubling jumps cost about 5.5 multiplications
+// per bit of each class length; the closed form about 1.5 per bit (the powers
+// M^t), 8 per class and 1.5 per bit of p (the one inversion), so short
+// prefixes -- a few classes of a few terms -- go by doubling.
+CTD_HD uint64_t smarandache_at(const Mont &m, uint64_t b, uint64_t s)
+{
+    uint32_t bits = 0, classes = 0;
+    for (uint64_t c = 1; c <= s;) {
+        uint64_t pw;
+        const uint64_t cend = class_end(b, c, pw);
+        const uint64_t last = cend - 1 < s ? cend - 1 : s;
+        bits += 64 - clz64(last - c + 1);
+        ++classes;
+        if (cend == ~0ull || cend > s)
+            break;
+        c = cend;
+    }
+    const uint32_t pbits = 64 - clz64(m.p);
+    // both sides doubled: 11 bits  vs  3 bits + 16 K + 3 log p
+    if (11 * bits <= 3 * bits + 16 * classes + 3 * pbits)
+        return smarandache_at_doubling(m, b, s);
+    return smarandache_at_closed(m, b, s);
 }
 
 }  // namespace ctd

@@ -112,14 +112,24 @@ typedef struct ctd_tuning {
     uint32_t items_per_thread; /* below this many (prime, tile) items per resident thread, index ranges are tiled */
     uint32_t min_tile;         /* shortest index tile (each tile starts with an O(log n) jump) */
     uint32_t segment_log2;     /* default prime-segment width of ctd_run_plain, log2; 0 = 26 */
-    uint32_t reserved[3];
+    uint32_t variant;          /* step form, CTD_VARIANT_* (results never depend on it) */
+    uint32_t reserved[2];
 } ctd_tuning;
+
+/* Step forms a tuning can select.  AUTO: the fastest measured form for the
+ * family and prime width.  WALK: the term-by-term walk (doubling and fixed-n
+ * families: no baby-step blocks; Smarandache: the 64-bit Shoup step instead
+ * of the 32-bit Barrett step).  MONTGOMERY: Smarandache steps in Montgomery
+ * form (the general path).  Families without such a choice ignore it. */
+#define CTD_VARIANT_AUTO 0
+#define CTD_VARIANT_WALK 1
+#define CTD_VARIANT_MONTGOMERY 2
 
 /* The parameters in force for `family` (defaults until tuned or set). */
 int ctd_get_tuning(ctd_ctx *ctx, uint32_t family, ctd_tuning *out);
 /* Sets them; NULL restores the defaults.  ctd_set_launch overrides still win. */
 int ctd_set_tuning(ctd_ctx *ctx, uint32_t family, const ctd_tuning *t);
-/* Autotuner: times candidate launch shapes and tilings of the job's family on
+/* Autotuner: times candidate launch shapes, tilings and step forms of the job's family on
  * the job's own first prime segment (its index range, a sample of its primes)
  * for about `budget_s` seconds, applies the fastest to the context and returns
  * it in *best.  Results never depend on the tuning, only the speed. */

@@ -89,7 +89,8 @@ def test_smarandache_jump_closed_form_and_doubling(sm_checker):
     inp = "".join(f"{p} {b} {s}\n" for p, b, s in cases)
     out = subprocess.run([sm_checker], input=inp, capture_output=True, text=True, check=True).stdout.split("\n")
     for (p, b, s), line in zip(cases, out):
-        closed, dbl = map(int, line.split())
+        closed, dbl, chosen = map(int, line.split())
         want = smarandache_mod(b, s, p)
         assert closed == want, (p, b, s)
         assert dbl == want, (p, b, s)
+        assert chosen == want, (p, b, s)

@@ -18,6 +18,8 @@ def run(eng, job):
     (O.PROTH, 3, 1, 20001, 1 << 32, (1 << 32) + (1 << 22)),
     (O.SMARANDACHE, 10, 500, 2500, 1 << 30, (1 << 30) + (1 << 22)),
     (O.TRIBONACCI, 0, 2, 6002, 1 << 20, 1 << 22),
+    (O.RIESEL_FIXED_N, 777, 3, 9003, 1 << 31, (1 << 31) + (1 << 22)),
+    (O.SMARANDACHE, 7, 1, 3001, 3, 1 << 20),
 ])
 def test_autotune_keeps_results(eng, case):
     fam, param, n0, n1, f0, f1 = case
@@ -29,17 +31,18 @@ def test_autotune_keeps_results(eng, case):
         assert best["ctas_per_sm"] >= 0 and best["items_per_thread"] > 0 and best["min_tile"] > 0
         assert eng.get_tuning(fam) == best
         assert run(eng, job) == want
-        # an extreme but valid shape: still the same factors
-        eng.set_tuning(fam, {"block_size": 64, "ctas_per_sm": 1, "items_per_thread": 32, "min_tile": 1024,
-                             "segment_log2": 22})
-        assert run(eng, job) == want
+        # an extreme but valid shape, and every step form: still the same factors
+        for variant in (0, 1, 2):
+            eng.set_tuning(fam, {"block_size": 64, "ctas_per_sm": 1, "items_per_thread": 32, "min_tile": 1024,
+                                 "segment_log2": 22, "variant": variant})
+            assert run(eng, job) == want, variant
     finally:
         eng.set_tuning(fam, None)
     assert eng.get_tuning(fam)["segment_log2"] == 26
 
 
 def test_set_tuning_rejects_bad_values(eng):
-    for bad in ({"block_size": 48}, {"block_size": 512}, {"items_per_thread": 0}, {"segment_log2": 50}):
+    for bad in ({"block_size": 48}, {"block_size": 512}, {"items_per_thread": 0}, {"segment_log2": 50}, {"variant": 3}):
         t = {"block_size": 256, "ctas_per_sm": 0, "items_per_thread": 8, "min_tile": 4096, "segment_log2": 0}
         t.update(bad)
         with pytest.raises(ctd.CtdError):
