@@ -191,6 +191,16 @@ __device__ __forceinline__ void walk_add63(uint64_t u, uint64_t c, uint64_t targ
     }
 }
 
+// p^-1 mod 2^32 for odd p (Newton-Hensel lifting from 3 correct bits)
+__device__ __forceinline__ uint32_t inverse_mod_2_32(uint32_t p)
+{
+    uint32_t x = p;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        x *= 2u - p * x;
+    return x;
+}
+
 // ------------------------------------------- baby-step / giant-step walks
 // For the recurrences whose step is an affine map of a single residue --
 // u -> 2u (Proth, Riesel, Mersenne) and v -> v + c (the fixed-n pair) -- the
@@ -617,9 +627,9 @@ __device__ __forceinline__ void run_tribonacci(const JobView &job, uint64_t p, u
 // quotient); SMALL: M < 2^32.  Returns the final x.
 template <bool SMALL>
 __device__ __forceinline__ uint64_t smarandache_walk64(const JobView &job, uint64_t p, uint64_t x, uint64_t M,
-                                                       uint64_t Ms, uint64_t mm, uint64_t mend, uint32_t plo,
-                                                       uint32_t p2lo)
+                                                       uint64_t Ms, uint64_t mm, uint64_t mend)
 {
+    const uint32_t pinv32 = inverse_mod_2_32((uint32_t)p);
     auto step = [&](uint64_t v, uint64_t mv) {
         const uint64_t q = mulhi64(v, Ms);
         const uint64_t vm = SMALL ? v * (uint64_t)(uint32_t)M : v * M;
@@ -631,7 +641,7 @@ __device__ __forceinline__ uint64_t smarandache_walk64(const JobView &job, uint6
 #pragma unroll
         for (int j = 0; j < UNROLL; ++j) {
             x = step(x, mm + j);
-            cand |= ((uint32_t)x == plo) | ((uint32_t)x == p2lo);
+            cand |= (uint32_t)x * pinv32 < 3u;  // low word of p or 2p (x >= 1)
         }
         if (cand) {
             uint64_t y = x0;
@@ -665,7 +675,9 @@ __device__ __forceinline__ uint64_t smarandache_walk_b32(const JobView &job, uin
 {
     const uint64_t np = (uint64_t)0 - p;
     const uint32_t nplo = (uint32_t)np, nphi = (uint32_t)(np >> 32);
-    const uint32_t plo = (uint32_t)p, p2lo = (uint32_t)(2 * p);
+    // x in {0, p, 2p} implies x_lo p^-1 = 0, 1 or 2 mod 2^32 (p^-1 mod 2^32):
+    // one multiply and one compare test the low word against all three
+    const uint32_t pinv32 = inverse_mod_2_32((uint32_t)p);
     auto step = [&](uint64_t v, uint64_t mv) {
         uint64_t T = (uint64_t)(uint32_t)v * M + mv;
         T += (uint64_t)((uint32_t)(v >> 32) * M) << 32;
@@ -681,8 +693,7 @@ __device__ __forceinline__ uint64_t smarandache_walk_b32(const JobView &job, uin
 #pragma unroll
         for (int j = 0; j < UNROLL; ++j) {
             x = step(x, mm + j);
-            const uint32_t lo = (uint32_t)x;
-            cand |= (lo == 0u) | (lo == plo) | (lo == p2lo);
+            cand |= (uint32_t)x * pinv32 < 3u;
         }
         if (cand) {
             uint64_t y = x0;
@@ -717,6 +728,7 @@ __device__ __forceinline__ void run_smarandache(const JobView &job, uint64_t p, 
         // 32-bit Shoup path: x kept in [0, 3p) (Shoup output < 2p, plus m < p),
         // so x = 0 mod p <=> x == p or x == 2p (x >= 1 after a step).
         const uint32_t p32 = (uint32_t)p, p2 = 2 * p32;
+        const uint32_t pinv32 = inverse_mod_2_32(p32);
         uint32_t x = (uint32_t)m.from(X);
         while (mcur < e) {
             uint64_t pw;
@@ -732,7 +744,7 @@ __device__ __forceinline__ void run_smarandache(const JobView &job, uint64_t p, 
                 for (int j = 0; j < UNROLL; ++j) {
                     uint32_t q = mulhi32(x, Ms);
                     x = x * M + (mm + j) - q * p32;
-                    cand |= (x == p32) | (x == p2);
+                    cand |= x * pinv32 < 3u;  // x in {p, 2p} => x p^-1 mod 2^32 in {1, 2}
                 }
                 if (cand) {
                     uint32_t y = x0;
@@ -762,7 +774,6 @@ __device__ __forceinline__ void run_smarandache(const JobView &job, uint64_t p, 
         // x = 0 mod p <=> x == p or x == 2p.  The unrolled body tests the low
         // words only; a block with a candidate is replayed with the full test.
         uint64_t x = m.from(X);
-        const uint32_t plo = (uint32_t)p, p2lo = (uint32_t)(2 * p);
         // Barrett-32 constants (p < 2^48): sh = floor(log2 p), mu = floor(2^(sh+32) / p)
         const uint32_t sh = 63 - clz64(p);
         uint32_t mu = 0;
@@ -783,9 +794,9 @@ __device__ __forceinline__ void run_smarandache(const JobView &job, uint64_t p, 
             else if (b32)
                 x = smarandache_walk_b32<false>(job, p, x, (uint32_t)M, sh, mu, mcur, mend);
             else if (M >> 32)
-                x = smarandache_walk64<false>(job, p, x, M, m.shoup(M), mcur, mend, plo, p2lo);
+                x = smarandache_walk64<false>(job, p, x, M, m.shoup(M), mcur, mend);
             else
-                x = smarandache_walk64<true>(job, p, x, M, m.shoup(M), mcur, mend, plo, p2lo);
+                x = smarandache_walk64<true>(job, p, x, M, m.shoup(M), mcur, mend);
             mcur = mend;
         }
         return;
