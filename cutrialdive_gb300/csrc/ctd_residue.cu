@@ -201,6 +201,53 @@ __device__ __forceinline__ uint32_t inverse_mod_2_32(uint32_t p)
     return x;
 }
 
+// ---------------------------------------------- lazily reduced blocks
+// For p < 2^40 the linear recurrences run a block of steps on unreduced
+// 64-bit values: from states below 3p, each step at most adds the previous
+// two (three) values, so after step j of a block every value is below
+// K[j] p, K growing like the recurrence itself (7752 p after 16 Fibonacci
+// steps, 6627 p after 12 tribonacci steps: below 2^53).  A value x = k p,
+// k < K[j], satisfies x_lo p^-1 = k mod 2^32, so "x_lo p^-1 mod 2^32 < K[j]"
+// (one multiply, one compare) flags every zero; false candidates come at
+// K[j] 2^-32 and are settled by an exact replay.  At the block's end each
+// state is brought back below 3p by a Barrett step from one 32-bit high
+// multiply (q = mulhi(x >> sh, mu) undershoots floor(x / p) by at most 2).
+struct Lazy {
+    uint64_t p;
+    uint32_t pinv32;  // p^-1 mod 2^32
+    uint32_t sh;      // floor(log2 p)
+    uint32_t mu;      // floor(2^(sh+32) / p)
+    uint32_t nplo, nphi;  // 2^64 - p
+
+    __device__ __forceinline__ void init(const Mont &m)
+    {
+        p = m.p;
+        pinv32 = inverse_mod_2_32((uint32_t)p);
+        sh = 63 - clz64(p);
+        const uint64_t mu64 = m.mu();
+        mu = sh <= 32 ? (uint32_t)(mu64 >> (32 - sh)) : (uint32_t)((mu64 << (sh - 32)) + ((m.one << (sh - 32)) / p));
+        const uint64_t np = (uint64_t)0 - p;
+        nplo = (uint32_t)np;
+        nphi = (uint32_t)(np >> 32);
+    }
+    // x < 2^(sh+32) -> a value = x mod p in [0, 3p)
+    __device__ __forceinline__ uint64_t reduce(uint64_t x) const
+    {
+        const uint32_t top = (uint32_t)(x >> sh);
+        const uint32_t q = __umulhi(top, mu);
+        uint64_t r = (uint64_t)q * nplo + x;
+        r += (uint64_t)(q * nphi) << 32;
+        return r;
+    }
+    // x < 3p -> x mod p
+    __device__ __forceinline__ uint64_t full(uint64_t x) const
+    {
+        x = x >= p ? x - p : x;
+        return x >= p ? x - p : x;
+    }
+    __device__ __forceinline__ bool maybe_zero(uint64_t x, uint32_t K) const { return (uint32_t)x * pinv32 < K; }
+};
+
 // ------------------------------------------- baby-step / giant-step walks
 // For the recurrences whose step is an affine map of a single residue --
 // u -> 2u (Proth, Riesel, Mersenne) and v -> v + c (the fixed-n pair) -- the
@@ -433,7 +480,48 @@ __device__ __forceinline__ void run_fibonacci(const JobView &job, uint64_t p, ui
     if (b == 0)
         push(job.fb, idx, p);
     uint64_t i = 0;
-    if (p < (1ull << 63)) {
+    if (p < (1ull << 40)) {
+        Mont mt;
+        mt.init_lite(p);
+        Lazy lz;
+        lz.init(mt);
+        constexpr int FB = 16;  // steps per block
+        // bounds K[j]: values after step j of a block are below K[j] p
+        constexpr uint32_t K[FB] = {6, 9, 15, 24, 39, 63, 102, 165, 267, 432, 699, 1131, 1830, 2961, 4791, 7752};
+        uint64_t nb = steps / FB;
+        while (nb) {
+          const uint32_t chunk = nb > 0x40000000ull ? 0x40000000u : (uint32_t)nb;
+          for (uint32_t bk = 0; bk < chunk; ++bk) {
+            const uint64_t a0 = a, b0 = b;
+            bool cand = false;
+#pragma unroll
+            for (int j = 0; j < FB; j += 2) {
+                a += b;  // (a, b) is (S(n-1), S(n)) again after every second step
+                cand |= lz.maybe_zero(a, K[j]);
+                b += a;
+                cand |= lz.maybe_zero(b, K[j + 1]);
+            }
+            if (cand) {
+                uint64_t x = lz.full(a0), y = lz.full(b0);
+                const uint64_t at = idx + i + (uint64_t)bk * FB;
+#pragma unroll 1
+                for (int j = 0; j < FB; ++j) {
+                    uint64_t c = add63(x, y, p);
+                    x = y;
+                    y = c;
+                    if (c == 0)
+                        push(job.fb, at + j + 1, p);
+                }
+            }
+            a = lz.reduce(a);
+            b = lz.reduce(b);
+          }
+          i += (uint64_t)chunk * FB;
+          nb -= chunk;
+        }
+        a = lz.full(a);
+        b = lz.full(b);
+    } else if (p < (1ull << 63)) {
         const uint32_t zero = 0;
         constexpr int FB = 16;  // steps per block
         // blocks of FB steps counted in 32-bit chunks; the state at a block's
@@ -562,7 +650,51 @@ __device__ __forceinline__ void run_tribonacci(const JobView &job, uint64_t p, u
         return;
     const uint64_t steps = len - 3;  // values T(s+3) .. T(e-1)
     uint64_t i = 0;                   // value T(s+3+i) goes to index idx+3+i
-    if (p < (1ull << 62)) {
+    if (p < (1ull << 40)) {
+        Lazy lz;
+        lz.init(m);
+        constexpr int TB = 12;  // steps per block
+        // bounds K[j]: values after step j of a block are below K[j] p
+        constexpr uint32_t K[TB] = {9, 15, 27, 51, 93, 171, 315, 579, 1065, 1959, 3603, 6627};
+        uint64_t nb = steps / TB;
+        while (nb) {
+          const uint32_t chunk = nb > 0x40000000ull ? 0x40000000u : (uint32_t)nb;
+          for (uint32_t bk = 0; bk < chunk; ++bk) {
+            const uint64_t x0 = x, y0 = y, z0 = z;
+            bool cand = false;
+#pragma unroll
+            for (int j = 0; j < TB; j += 3) {
+                x += y + z;  // T(k+3) replaces T(k): the roles rotate every step
+                cand |= lz.maybe_zero(x, K[j]);
+                y += z + x;
+                cand |= lz.maybe_zero(y, K[j + 1]);
+                z += x + y;
+                cand |= lz.maybe_zero(z, K[j + 2]);
+            }
+            if (cand) {
+                uint64_t a = lz.full(x0), b = lz.full(y0), c = lz.full(z0);
+                const uint64_t at = idx + 3 + i + (uint64_t)bk * TB;
+#pragma unroll 1
+                for (int j = 0; j < TB; ++j) {
+                    uint64_t w = trib_add(a, b, c, p);
+                    a = b;
+                    b = c;
+                    c = w;
+                    if (w == 0)
+                        push(job.fb, at + j, p);
+                }
+            }
+            x = lz.reduce(x);
+            y = lz.reduce(y);
+            z = lz.reduce(z);
+          }
+          i += (uint64_t)chunk * TB;
+          nb -= chunk;
+        }
+        x = lz.full(x);
+        y = lz.full(y);
+        z = lz.full(z);
+    } else if (p < (1ull << 62)) {
         constexpr int TB = 12;  // steps per block
         const uint32_t zero = 0;
         const uint64_t p2 = 2 * p;
@@ -629,7 +761,7 @@ template <bool SMALL>
 __device__ __forceinline__ uint64_t smarandache_walk64(const JobView &job, uint64_t p, uint64_t x, uint64_t M,
                                                        uint64_t Ms, uint64_t mm, uint64_t mend)
 {
-    const uint32_t pinv32 = inverse_mod_2_32((uint32_t)p);
+    const uint32_t plo = (uint32_t)p, p2lo = (uint32_t)(2 * p);
     auto step = [&](uint64_t v, uint64_t mv) {
         const uint64_t q = mulhi64(v, Ms);
         const uint64_t vm = SMALL ? v * (uint64_t)(uint32_t)M : v * M;
@@ -641,7 +773,7 @@ __device__ __forceinline__ uint64_t smarandache_walk64(const JobView &job, uint6
 #pragma unroll
         for (int j = 0; j < UNROLL; ++j) {
             x = step(x, mm + j);
-            cand |= (uint32_t)x * pinv32 < 3u;  // low word of p or 2p (x >= 1)
+            cand |= ((uint32_t)x == plo) | ((uint32_t)x == p2lo);
         }
         if (cand) {
             uint64_t y = x0;
@@ -675,9 +807,9 @@ __device__ __forceinline__ uint64_t smarandache_walk_b32(const JobView &job, uin
 {
     const uint64_t np = (uint64_t)0 - p;
     const uint32_t nplo = (uint32_t)np, nphi = (uint32_t)(np >> 32);
-    // x in {0, p, 2p} implies x_lo p^-1 = 0, 1 or 2 mod 2^32 (p^-1 mod 2^32):
-    // one multiply and one compare test the low word against all three
-    const uint32_t pinv32 = inverse_mod_2_32((uint32_t)p);
+    // low words of p and 2p (the multiply pipe bounds this walk, so the zero
+    // test stays three compares on the ALU rather than one multiply)
+    const uint32_t plo = (uint32_t)p, p2lo = (uint32_t)(2 * p);
     auto step = [&](uint64_t v, uint64_t mv) {
         uint64_t T = (uint64_t)(uint32_t)v * M + mv;
         T += (uint64_t)((uint32_t)(v >> 32) * M) << 32;
@@ -693,7 +825,8 @@ __device__ __forceinline__ uint64_t smarandache_walk_b32(const JobView &job, uin
 #pragma unroll
         for (int j = 0; j < UNROLL; ++j) {
             x = step(x, mm + j);
-            cand |= (uint32_t)x * pinv32 < 3u;
+            const uint32_t lo = (uint32_t)x;
+            cand |= (lo == 0u) | (lo == plo) | (lo == p2lo);
         }
         if (cand) {
             uint64_t y = x0;
@@ -728,7 +861,6 @@ __device__ __forceinline__ void run_smarandache(const JobView &job, uint64_t p, 
         // 32-bit Shoup path: x kept in [0, 3p) (Shoup output < 2p, plus m < p),
         // so x = 0 mod p <=> x == p or x == 2p (x >= 1 after a step).
         const uint32_t p32 = (uint32_t)p, p2 = 2 * p32;
-        const uint32_t pinv32 = inverse_mod_2_32(p32);
         uint32_t x = (uint32_t)m.from(X);
         while (mcur < e) {
             uint64_t pw;
@@ -744,7 +876,7 @@ __device__ __forceinline__ void run_smarandache(const JobView &job, uint64_t p, 
                 for (int j = 0; j < UNROLL; ++j) {
                     uint32_t q = mulhi32(x, Ms);
                     x = x * M + (mm + j) - q * p32;
-                    cand |= x * pinv32 < 3u;  // x in {p, 2p} => x p^-1 mod 2^32 in {1, 2}
+                    cand |= (x == p32) | (x == p2);
                 }
                 if (cand) {
                     uint32_t y = x0;
@@ -831,12 +963,12 @@ __device__ __forceinline__ void run_peano(const JobView &job, uint64_t p, uint64
     }
 }
 
-// Resident CTAs of 256 threads the register budget is sized for: the
-// baby-step families keep 32 targets in registers, Smarandache and
-// tribonacci carry wider state.
+// Resident CTAs of 256 threads the register budget is sized for (64
+// registers a thread): the baby-step families keep 32 targets in registers,
+// the others carry block-start copies and reduction constants.
 constexpr int min_ctas_per_sm(uint32_t fam)
 {
-    return (fam == FIBONACCI || fam == LUCAS || fam == PEANO) ? 6 : 4;
+    return fam == PEANO ? 6 : 4;
 }
 
 template <uint32_t FAM>
