@@ -84,13 +84,16 @@ FAMILY_NAMES = {0: "MERSENNE", 1: "PROTH", 2: "RIESEL", 3: "SMARANDACHE", 4: "FI
 #    (u 2^-32, a 32-bit Montgomery reduction) is 4 multiply-pipe
 #    instructions -> 32/32 ALU ops;
 #  * fixed-n: the same blocks, giant step a modular add (5 ALU ops) -> 37/32;
-#  * Fibonacci/Lucas: modular add (2 add, 1 sign test, 2 predicated add) +
-#    1 compare = 6;
-#  * tribonacci: two-term add and -2p (4), two sign tests and predicated
-#    adds (6), compare (1) = 11;
+#  * Fibonacci/Lucas (p < 2^40): lazily reduced blocks of 16 steps: a 64-bit
+#    add (2) and the zero-test compare (1) per step, plus one shift per state
+#    for the block-end reduction (2 per 16 steps) -> 3.125; the test's
+#    multiply and the reduction's multiply-adds run on the multiply pipe;
+#  * tribonacci (p < 2^40): blocks of 12 steps: a three-input 64-bit add (2)
+#    and the compare (1) per step, 3 shifts per block -> 3.25;
 #  * Smarandache (64-bit Shoup): adds/subtracts of x M + m - q p (4) and
 #    two low-word compares = 6, plus 9 32-bit multiplies.
-ALU_OPS_PER_UPDATE = {0: 32 / 32, 1: 32 / 32, 2: 32 / 32, 6: 37 / 32, 7: 37 / 32, 4: 6, 5: 6, 8: 11, 3: 6}
+ALU_OPS_PER_UPDATE = {0: 32 / 32, 1: 32 / 32, 2: 32 / 32, 6: 37 / 32, 7: 37 / 32, 4: 50 / 16, 5: 50 / 16, 8: 39 / 12,
+                      3: 6}
 # DRAM bytes per prime of residue_kernel<PROTH> from one ncu capture on
 # [2^32, 2^32 + 2^27): 48,436,480 + 1,024 bytes for 6,047,768 primes; each
 # prime is read once per launch, so a full launch's traffic is this figure

@@ -245,7 +245,6 @@ struct Lazy {
         x = x >= p ? x - p : x;
         return x >= p ? x - p : x;
     }
-    __device__ __forceinline__ bool maybe_zero(uint64_t x, uint32_t K) const { return (uint32_t)x * pinv32 < K; }
 };
 
 // ------------------------------------------- baby-step / giant-step walks
@@ -486,22 +485,36 @@ __device__ __forceinline__ void run_fibonacci(const JobView &job, uint64_t p, ui
         Lazy lz;
         lz.init(mt);
         constexpr int FB = 16;  // steps per block
-        // bounds K[j]: values after step j of a block are below K[j] p
-        constexpr uint32_t K[FB] = {6, 9, 15, 24, 39, 63, 102, 165, 267, 432, 699, 1131, 1830, 2961, 4791, 7752};
+        // bounds K[j] (in the PTX below): values after step j of a block are
+        // below K[j] p = 6, 9, 15, 24, ... 7752 p (from states below 3p)
         uint64_t nb = steps / FB;
         while (nb) {
           const uint32_t chunk = nb > 0x40000000ull ? 0x40000000u : (uint32_t)nb;
           for (uint32_t bk = 0; bk < chunk; ++bk) {
             const uint64_t a0 = a, b0 = b;
-            bool cand = false;
-#pragma unroll
-            for (int j = 0; j < FB; j += 2) {
-                a += b;  // (a, b) is (S(n-1), S(n)) again after every second step
-                cand |= lz.maybe_zero(a, K[j]);
-                b += a;
-                cand |= lz.maybe_zero(b, K[j + 1]);
-            }
-            if (cand) {
+            uint32_t cand;
+            // a <- a + b, b <- b + a alternately ((a, b) is (S(n-1), S(n))
+            // again after every second step); after each add the low word
+            // times p^-1 is compared with the step's bound K[j].
+            // operands: %0 = a, %1 = b, %2 = candidate flag, %3 = p^-1 mod 2^32
+#define CTD_LZ_STEP(X, Y, KJ)                                                                  \
+    "add.u64 " X ", " X ", " Y ";\n\tmov.b64 {lo, hi}, " X ";\n\tmul.lo.u32 t, lo, %3;\n\t"   \
+    "setp.lt.or.u32 c, t, " #KJ ", c;\n\t"
+            asm("{\n\t.reg .pred c;\n\t.reg .b32 lo, hi, t;\n\tsetp.ne.u32 c, %3, %3;\n\t"
+                CTD_LZ_STEP("%0", "%1", 6) CTD_LZ_STEP("%1", "%0", 9) CTD_LZ_STEP("%0", "%1", 15)
+                CTD_LZ_STEP("%1", "%0", 24) CTD_LZ_STEP("%0", "%1", 39) CTD_LZ_STEP("%1", "%0", 63)
+                CTD_LZ_STEP("%0", "%1", 102) CTD_LZ_STEP("%1", "%0", 165) CTD_LZ_STEP("%0", "%1", 267)
+                CTD_LZ_STEP("%1", "%0", 432) CTD_LZ_STEP("%0", "%1", 699) CTD_LZ_STEP("%1", "%0", 1131)
+                CTD_LZ_STEP("%0", "%1", 1830) CTD_LZ_STEP("%1", "%0", 2961) CTD_LZ_STEP("%0", "%1", 4791)
+                CTD_LZ_STEP("%1", "%0", 7752)
+                "selp.u32 %2, 1, 0, c;\n\t}"
+                : "+l"(a), "+l"(b), "=r"(cand)
+                : "r"(lz.pinv32));
+#undef CTD_LZ_STEP
+            // the converged lanes replay together when any of them has a
+            // candidate: a replay taken by some lanes only would leave the
+            // warp diverged for the rest of the walk
+            if (__any_sync(__activemask(), cand)) {
                 uint64_t x = lz.full(a0), y = lz.full(b0);
                 const uint64_t at = idx + i + (uint64_t)bk * FB;
 #pragma unroll 1
@@ -654,24 +667,31 @@ __device__ __forceinline__ void run_tribonacci(const JobView &job, uint64_t p, u
         Lazy lz;
         lz.init(m);
         constexpr int TB = 12;  // steps per block
-        // bounds K[j]: values after step j of a block are below K[j] p
-        constexpr uint32_t K[TB] = {9, 15, 27, 51, 93, 171, 315, 579, 1065, 1959, 3603, 6627};
+        // bounds K[j] (in the PTX below): values after step j of a block are
+        // below K[j] p = 9, 15, 27, 51, ... 6627 p (from states below 3p)
         uint64_t nb = steps / TB;
         while (nb) {
           const uint32_t chunk = nb > 0x40000000ull ? 0x40000000u : (uint32_t)nb;
           for (uint32_t bk = 0; bk < chunk; ++bk) {
             const uint64_t x0 = x, y0 = y, z0 = z;
-            bool cand = false;
-#pragma unroll
-            for (int j = 0; j < TB; j += 3) {
-                x += y + z;  // T(k+3) replaces T(k): the roles rotate every step
-                cand |= lz.maybe_zero(x, K[j]);
-                y += z + x;
-                cand |= lz.maybe_zero(y, K[j + 1]);
-                z += x + y;
-                cand |= lz.maybe_zero(z, K[j + 2]);
-            }
-            if (cand) {
+            uint32_t cand;
+            // T(k+3) replaces T(k): the roles rotate every step
+            // operands: %0..%2 = x, y, z, %3 = candidate flag, %4 = p^-1 mod 2^32
+#define CTD_LZ3_STEP(X, Y, Z, KJ)                                                                         \
+    "add.u64 " X ", " X ", " Y ";\n\tadd.u64 " X ", " X ", " Z ";\n\tmov.b64 {lo, hi}, " X ";\n\t"     \
+    "mul.lo.u32 t, lo, %4;\n\tsetp.lt.or.u32 c, t, " #KJ ", c;\n\t"
+            asm("{\n\t.reg .pred c;\n\t.reg .b32 lo, hi, t;\n\tsetp.ne.u32 c, %4, %4;\n\t"
+                CTD_LZ3_STEP("%0", "%1", "%2", 9) CTD_LZ3_STEP("%1", "%2", "%0", 15)
+                CTD_LZ3_STEP("%2", "%0", "%1", 27) CTD_LZ3_STEP("%0", "%1", "%2", 51)
+                CTD_LZ3_STEP("%1", "%2", "%0", 93) CTD_LZ3_STEP("%2", "%0", "%1", 171)
+                CTD_LZ3_STEP("%0", "%1", "%2", 315) CTD_LZ3_STEP("%1", "%2", "%0", 579)
+                CTD_LZ3_STEP("%2", "%0", "%1", 1065) CTD_LZ3_STEP("%0", "%1", "%2", 1959)
+                CTD_LZ3_STEP("%1", "%2", "%0", 3603) CTD_LZ3_STEP("%2", "%0", "%1", 6627)
+                "selp.u32 %3, 1, 0, c;\n\t}"
+                : "+l"(x), "+l"(y), "+l"(z), "=r"(cand)
+                : "r"(lz.pinv32));
+#undef CTD_LZ3_STEP
+            if (__any_sync(__activemask(), cand)) {  // lanes replay together (see the Fibonacci block)
                 uint64_t a = lz.full(x0), b = lz.full(y0), c = lz.full(z0);
                 const uint64_t at = idx + 3 + i + (uint64_t)bk * TB;
 #pragma unroll 1
