@@ -179,3 +179,27 @@ def test_hits_divide_terms_at_scale(eng):
     for n, p in hits:
         assert (3 * pow(2, n, p) + 1) % p == 0
         assert f0 <= p < f1
+
+
+@pytest.mark.parametrize("family,n0,n1", [(O.FIBONACCI, 1, 2501), (O.LUCAS, 3, 1003), (O.TRIBONACCI, 2, 1502),
+                                          (O.FIBONACCI, 7, 40)])
+def test_linear_recurrences_across_the_lazy_block_limit(eng, family, n0, n1):
+    """Primes on both sides of 2^40, where the lazily reduced blocks give way to
+    the modular-add walk; index ranges with and without a partial last block."""
+    f0, f1 = (1 << 40) - (1 << 17), (1 << 40) + (1 << 17)
+    got = run_gpu(eng, family, 0, n0, n1, f0, f1)
+    want = O.trial_factor(family, 0, n0, n1, f0, f1, max_factors=32)
+    assert got.counts.tolist() == want.counts.tolist()
+    assert text(got) == want.format()
+
+
+@pytest.mark.parametrize("family,param", [(O.PROTH, 1279), (O.RIESEL, 3), (O.MERSENNE, 0), (O.PROTH_FIXED_N, 77),
+                                          (O.RIESEL_FIXED_N, 5)])
+def test_baby_step_blocks_tail_and_short_ranges(eng, family, param):
+    """Index ranges of 1..200 terms (below, at and above two 32-term blocks) so
+    the block walk, its tail and the term-by-term walk all run."""
+    f0, f1 = (1 << 33), (1 << 33) + (1 << 18)
+    for n0, n1 in [(5, 6), (5, 68), (5, 69), (5, 70), (1000, 1063), (1000, 1200)]:
+        got = run_gpu(eng, family, param, n0, n1, f0, f1)
+        want = O.trial_factor(family, param, n0, n1, f0, f1, max_factors=32)
+        assert text(got) == want.format(), (n0, n1)
