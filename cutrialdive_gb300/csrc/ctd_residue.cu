@@ -491,7 +491,6 @@ __device__ __forceinline__ void run_fibonacci(const JobView &job, uint64_t p, ui
         while (nb) {
           const uint32_t chunk = nb > 0x40000000ull ? 0x40000000u : (uint32_t)nb;
           for (uint32_t bk = 0; bk < chunk; ++bk) {
-            const uint64_t a0 = a, b0 = b;
             uint32_t cand;
             // a <- a + b, b <- b + a alternately ((a, b) is (S(n-1), S(n))
             // again after every second step); after each add the low word
@@ -515,7 +514,17 @@ __device__ __forceinline__ void run_fibonacci(const JobView &job, uint64_t p, ui
             // candidate: a replay taken by some lanes only would leave the
             // warp diverged for the rest of the walk
             if (__any_sync(__activemask(), cand)) {
-                uint64_t x = lz.full(a0), y = lz.full(b0);
+                // the block's values are exact integers: undo its FB adds to
+                // recover the start, reduce it, and replay with the full test
+                uint64_t x = a, y = b;
+#pragma unroll 1
+                for (int j = 0; j < FB; ++j) {
+                    const uint64_t w = y - x;
+                    y = x;
+                    x = w;
+                }
+                x = lz.full(x);
+                y = lz.full(y);
                 const uint64_t at = idx + i + (uint64_t)bk * FB;
 #pragma unroll 1
                 for (int j = 0; j < FB; ++j) {
@@ -673,7 +682,6 @@ __device__ __forceinline__ void run_tribonacci(const JobView &job, uint64_t p, u
         while (nb) {
           const uint32_t chunk = nb > 0x40000000ull ? 0x40000000u : (uint32_t)nb;
           for (uint32_t bk = 0; bk < chunk; ++bk) {
-            const uint64_t x0 = x, y0 = y, z0 = z;
             uint32_t cand;
             // T(k+3) replaces T(k): the roles rotate every step
             // operands: %0..%2 = x, y, z, %3 = candidate flag, %4 = p^-1 mod 2^32
@@ -692,7 +700,18 @@ __device__ __forceinline__ void run_tribonacci(const JobView &job, uint64_t p, u
                 : "r"(lz.pinv32));
 #undef CTD_LZ3_STEP
             if (__any_sync(__activemask(), cand)) {  // lanes replay together (see the Fibonacci block)
-                uint64_t a = lz.full(x0), b = lz.full(y0), c = lz.full(z0);
+                // exact integers within the block: undo its TB adds
+                uint64_t a = x, b = y, c = z;
+#pragma unroll 1
+                for (int j = 0; j < TB; ++j) {
+                    const uint64_t w = c - b - a;
+                    c = b;
+                    b = a;
+                    a = w;
+                }
+                a = lz.full(a);
+                b = lz.full(b);
+                c = lz.full(c);
                 const uint64_t at = idx + 3 + i + (uint64_t)bk * TB;
 #pragma unroll 1
                 for (int j = 0; j < TB; ++j) {
