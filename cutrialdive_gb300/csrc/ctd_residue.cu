@@ -683,23 +683,18 @@ __device__ __forceinline__ void run_tribonacci(const JobView &job, uint64_t p, u
           const uint32_t chunk = nb > 0x40000000ull ? 0x40000000u : (uint32_t)nb;
           for (uint32_t bk = 0; bk < chunk; ++bk) {
             uint32_t cand;
-            // T(n+1) = 2 T(n) - T(n-3) (subtract the tribonacci identities for
-            // T(n+1) and T(n)): one three-input add per step over a window of
-            // four values W, X, Y, Z = T(k-1) .. T(k+2), the oldest overwritten;
-            // W = Z - Y - X starts the window (it may be negative, the values
-            // the block produces are the exact non-negative sums).
+            // T(k+3) replaces T(k): the roles rotate every step
             // operands: %0..%2 = x, y, z, %3 = candidate flag, %4 = p^-1 mod 2^32
-#define CTD_LZ3_STEP(D, S, KJ)                                                                            \
-    "add.u64 d, " S ", " S ";\n\tsub.u64 " D ", d, " D ";\n\tmov.b64 {lo, hi}, " D ";\n\t"             \
+#define CTD_LZ3_STEP(X, Y, Z, KJ)                                                                         \
+    "add.u64 " X ", " X ", " Y ";\n\tadd.u64 " X ", " X ", " Z ";\n\tmov.b64 {lo, hi}, " X ";\n\t"     \
     "mul.lo.u32 t, lo, %4;\n\tsetp.lt.or.u32 c, t, " #KJ ", c;\n\t"
-            asm("{\n\t.reg .pred c;\n\t.reg .b32 lo, hi, t;\n\t.reg .b64 w, d;\n\tsetp.ne.u32 c, %4, %4;\n\t"
-                "sub.u64 w, %2, %1;\n\tsub.u64 w, w, %0;\n\t"
-                CTD_LZ3_STEP("w", "%2", 9) CTD_LZ3_STEP("%0", "w", 15)
-                CTD_LZ3_STEP("%1", "%0", 27) CTD_LZ3_STEP("%2", "%1", 51)
-                CTD_LZ3_STEP("w", "%2", 93) CTD_LZ3_STEP("%0", "w", 171)
-                CTD_LZ3_STEP("%1", "%0", 315) CTD_LZ3_STEP("%2", "%1", 579)
-                CTD_LZ3_STEP("w", "%2", 1065) CTD_LZ3_STEP("%0", "w", 1959)
-                CTD_LZ3_STEP("%1", "%0", 3603) CTD_LZ3_STEP("%2", "%1", 6627)
+            asm("{\n\t.reg .pred c;\n\t.reg .b32 lo, hi, t;\n\tsetp.ne.u32 c, %4, %4;\n\t"
+                CTD_LZ3_STEP("%0", "%1", "%2", 9) CTD_LZ3_STEP("%1", "%2", "%0", 15)
+                CTD_LZ3_STEP("%2", "%0", "%1", 27) CTD_LZ3_STEP("%0", "%1", "%2", 51)
+                CTD_LZ3_STEP("%1", "%2", "%0", 93) CTD_LZ3_STEP("%2", "%0", "%1", 171)
+                CTD_LZ3_STEP("%0", "%1", "%2", 315) CTD_LZ3_STEP("%1", "%2", "%0", 579)
+                CTD_LZ3_STEP("%2", "%0", "%1", 1065) CTD_LZ3_STEP("%0", "%1", "%2", 1959)
+                CTD_LZ3_STEP("%1", "%2", "%0", 3603) CTD_LZ3_STEP("%2", "%0", "%1", 6627)
                 "selp.u32 %3, 1, 0, c;\n\t}"
                 : "+l"(x), "+l"(y), "+l"(z), "=r"(cand)
                 : "r"(lz.pinv32));
