@@ -672,7 +672,87 @@ __device__ __forceinline__ void run_tribonacci(const JobView &job, uint64_t p, u
         return;
     const uint64_t steps = len - 3;  // values T(s+3) .. T(e-1)
     uint64_t i = 0;                   // value T(s+3+i) goes to index idx+3+i
-    if (p < (1ull << 40)) {
+    if (p < (1ull << 36)) {
+        // The lazily reduced blocks below, with each value held as two
+        // carry-free 32-bit limbs v = h 2^19 + l: from states below 3p < 2^38
+        // (l < 2^19, h < 2^19) twelve steps keep l < 2^31 and h < 2^31, so a
+        // step is one three-input 32-bit add per limb, and the zero test
+        // l p^-1 + h (2^19 p^-1) mod 2^32 < K[j] runs on the multiply pipe.
+        Lazy lz;
+        lz.init(m);
+        constexpr int TB = 12;  // steps per block
+        constexpr uint32_t LOW = (1u << 19) - 1;
+        const uint32_t c19 = lz.pinv32 << 19;  // 2^19 p^-1 mod 2^32
+        uint32_t xl = (uint32_t)x & LOW, xh = (uint32_t)(x >> 19);
+        uint32_t yl = (uint32_t)y & LOW, yh = (uint32_t)(y >> 19);
+        uint32_t zl = (uint32_t)z & LOW, zh = (uint32_t)(z >> 19);
+        uint64_t nb = steps / TB;
+        while (nb) {
+          const uint32_t chunk = nb > 0x40000000ull ? 0x40000000u : (uint32_t)nb;
+          for (uint32_t bk = 0; bk < chunk; ++bk) {
+            uint32_t cand;
+            // operands: %0..%5 = xl, xh, yl, yh, zl, zh, %6 = candidate flag,
+            // %7 = p^-1 mod 2^32, %8 = 2^19 p^-1 mod 2^32
+#define CTD_LZ2_STEP(XL, XH, YL, YH, ZL, ZH, KJ)                                                          \
+    "add.u32 " XL ", " XL ", " YL ";\n\tadd.u32 " XL ", " XL ", " ZL ";\n\t"                            \
+    "add.u32 " XH ", " XH ", " YH ";\n\tadd.u32 " XH ", " XH ", " ZH ";\n\t"                            \
+    "mul.lo.u32 t, " XH ", %8;\n\tmad.lo.u32 t, " XL ", %7, t;\n\tsetp.lt.or.u32 c, t, " #KJ ", c;\n\t"
+#define CTD_LZ2_X(KJ) CTD_LZ2_STEP("%0", "%1", "%2", "%3", "%4", "%5", KJ)
+#define CTD_LZ2_Y(KJ) CTD_LZ2_STEP("%2", "%3", "%4", "%5", "%0", "%1", KJ)
+#define CTD_LZ2_Z(KJ) CTD_LZ2_STEP("%4", "%5", "%0", "%1", "%2", "%3", KJ)
+            asm("{\n\t.reg .pred c;\n\t.reg .b32 t;\n\tsetp.ne.u32 c, %7, %7;\n\t"
+                CTD_LZ2_X(9) CTD_LZ2_Y(15) CTD_LZ2_Z(27) CTD_LZ2_X(51) CTD_LZ2_Y(93) CTD_LZ2_Z(171)
+                CTD_LZ2_X(315) CTD_LZ2_Y(579) CTD_LZ2_Z(1065) CTD_LZ2_X(1959) CTD_LZ2_Y(3603) CTD_LZ2_Z(6627)
+                "selp.u32 %6, 1, 0, c;\n\t}"
+                : "+r"(xl), "+r"(xh), "+r"(yl), "+r"(yh), "+r"(zl), "+r"(zh), "=r"(cand)
+                : "r"(lz.pinv32), "r"(c19));
+#undef CTD_LZ2_X
+#undef CTD_LZ2_Y
+#undef CTD_LZ2_Z
+#undef CTD_LZ2_STEP
+            x = ((uint64_t)xh << 19) + xl;
+            y = ((uint64_t)yh << 19) + yl;
+            z = ((uint64_t)zh << 19) + zl;
+            if (__any_sync(__activemask(), cand)) {  // lanes replay together (see the Fibonacci block)
+                uint64_t a = x, b = y, c = z;  // exact integers: undo the block's TB adds
+#pragma unroll 1
+                for (int j = 0; j < TB; ++j) {
+                    const uint64_t w = c - b - a;
+                    c = b;
+                    b = a;
+                    a = w;
+                }
+                a = lz.full(a);
+                b = lz.full(b);
+                c = lz.full(c);
+                const uint64_t at = idx + 3 + i + (uint64_t)bk * TB;
+#pragma unroll 1
+                for (int j = 0; j < TB; ++j) {
+                    uint64_t w = trib_add(a, b, c, p);
+                    a = b;
+                    b = c;
+                    c = w;
+                    if (w == 0)
+                        push(job.fb, at + j, p);
+                }
+            }
+            x = lz.reduce(x);
+            y = lz.reduce(y);
+            z = lz.reduce(z);
+            xl = (uint32_t)x & LOW;
+            xh = (uint32_t)(x >> 19);
+            yl = (uint32_t)y & LOW;
+            yh = (uint32_t)(y >> 19);
+            zl = (uint32_t)z & LOW;
+            zh = (uint32_t)(z >> 19);
+          }
+          i += (uint64_t)chunk * TB;
+          nb -= chunk;
+        }
+        x = lz.full(((uint64_t)xh << 19) + xl);
+        y = lz.full(((uint64_t)yh << 19) + yl);
+        z = lz.full(((uint64_t)zh << 19) + zl);
+    } else if (p < (1ull << 40)) {
         Lazy lz;
         lz.init(m);
         constexpr int TB = 12;  // steps per block
