@@ -261,17 +261,21 @@ struct Lazy {
 // runs on the multiply pipe.  A block whose low words matched is replayed
 // term by term with the full test, so results are those of the walk.
 constexpr int BS = 32;
+// terms per block of the doubling families (32 or 64: 64 targets halve the
+// per-block overhead per term but need twice the target registers)
+constexpr int DBS = 32;
 
 // halving mod odd p < 2^63: x/2 or (x + p)/2
 __device__ __forceinline__ uint64_t half63(uint64_t x, uint64_t p) { return (x + ((x & 1) ? p : 0)) >> 1; }
 
-// Nonzero iff lo equals one of the BS = 32 targets t[]: 32 predicate-
+// Nonzero iff lo equals one of the 32 targets t[K .. K+31]: 32 predicate-
 // accumulating compares (one ALU instruction each) in four independent
 // chains, merged into one flag.
 #define CTD_M4(A, B, C, D)                                                                        \
     "setp.eq.or.u32 c0, %1, %" #A ", c0;\n\tsetp.eq.or.u32 c1, %1, %" #B ", c1;\n\t"           \
     "setp.eq.or.u32 c2, %1, %" #C ", c2;\n\tsetp.eq.or.u32 c3, %1, %" #D ", c3;\n\t"
-__device__ __forceinline__ uint32_t match32(uint32_t lo, const uint32_t (&t)[BS])
+template <int K = 0, int N = BS>
+__device__ __forceinline__ uint32_t match32(uint32_t lo, const uint32_t (&t)[N])
 {
     uint32_t f;
     asm("{\n\t.reg .pred c<4>;\n\t"
@@ -282,10 +286,10 @@ __device__ __forceinline__ uint32_t match32(uint32_t lo, const uint32_t (&t)[BS]
         "or.pred c0, c0, c1;\n\tor.pred c2, c2, c3;\n\tor.pred c0, c0, c2;\n\t"
         "selp.u32 %0, 1, 0, c0;\n\t}"
         : "=r"(f)
-        : "r"(lo), "r"(t[0]), "r"(t[1]), "r"(t[2]), "r"(t[3]), "r"(t[4]), "r"(t[5]), "r"(t[6]), "r"(t[7]),
-          "r"(t[8]), "r"(t[9]), "r"(t[10]), "r"(t[11]), "r"(t[12]), "r"(t[13]), "r"(t[14]), "r"(t[15]),
-          "r"(t[16]), "r"(t[17]), "r"(t[18]), "r"(t[19]), "r"(t[20]), "r"(t[21]), "r"(t[22]), "r"(t[23]),
-          "r"(t[24]), "r"(t[25]), "r"(t[26]), "r"(t[27]), "r"(t[28]), "r"(t[29]), "r"(t[30]), "r"(t[31]));
+        : "r"(lo), "r"(t[K + 0]), "r"(t[K + 1]), "r"(t[K + 2]), "r"(t[K + 3]), "r"(t[K + 4]), "r"(t[K + 5]), "r"(t[K + 6]), "r"(t[K + 7]),
+          "r"(t[K + 8]), "r"(t[K + 9]), "r"(t[K + 10]), "r"(t[K + 11]), "r"(t[K + 12]), "r"(t[K + 13]), "r"(t[K + 14]), "r"(t[K + 15]),
+          "r"(t[K + 16]), "r"(t[K + 17]), "r"(t[K + 18]), "r"(t[K + 19]), "r"(t[K + 20]), "r"(t[K + 21]), "r"(t[K + 22]), "r"(t[K + 23]),
+          "r"(t[K + 24]), "r"(t[K + 25]), "r"(t[K + 26]), "r"(t[K + 27]), "r"(t[K + 28]), "r"(t[K + 29]), "r"(t[K + 30]), "r"(t[K + 31]));
     return f;
 }
 #undef CTD_M4
@@ -317,7 +321,6 @@ __device__ __forceinline__ void run_doubling(const JobView &job, uint64_t p, uin
     m.init_lite(p);
     const uint64_t target = (FAM == PROTH) ? p - 1 : 1;
     const uint64_t steps = e - s - 1;
-    const uint64_t nblk = (e - s) / BS;
     // u(s) = k 2^s mod p, for the per-step walks
     auto start = [&]() {
         const uint64_t U = m.pow2(s);  // 2^s in Montgomery form
@@ -327,7 +330,7 @@ __device__ __forceinline__ void run_doubling(const JobView &job, uint64_t p, uin
         const uint64_t k = job.param < p ? job.param : job.param % p;
         return m.mul(U, k);
     };
-    if (p < (1ull << 63) && nblk >= 2 && job.variant != CTD_VARIANT_WALK) {
+    if (p < (1ull << 63) && (e - s) / DBS >= 2 && job.variant != CTD_VARIANT_WALK) {
         // Walk w(n) = 2^-n instead: k 2^n = -1 (Proth) / 1 (Riesel, Mersenne
         // with k = 1) mod p iff w(n) = -k / k, a fixed target, and the giant
         // step w -> w 2^-32 is one reduction on the multiply pipe (redc32).
@@ -336,39 +339,47 @@ __device__ __forceinline__ void run_doubling(const JobView &job, uint64_t p, uin
         const uint64_t wt = (FAM == PROTH) ? (k ? p - k : 0) : k;  // target of w
         const uint64_t sr = s < p - 1 ? s : s % (p - 1);
         uint64_t w = m.from(m.pow2(p - 1 - sr));  // 2^-s mod p (Fermat)
-        uint32_t tlo[BS];
+        const uint64_t nb = (e - s) / DBS;
+        uint32_t tlo[DBS];
         uint64_t t = wt;
 #pragma unroll
-        for (int j = 0; j < BS; ++j) {
+        for (int j = 0; j < DBS; ++j) {
             tlo[j] = (uint32_t)t;
             t = add63(t, t, p);
         }
         const uint32_t plo = (uint32_t)p, phi = (uint32_t)(p >> 32), pinv32 = (uint32_t)m.pinv;
         const uint32_t one = (uint32_t)(p & 1);
         uint64_t at0 = s - job.n0;  // index of the current chunk's first term
-        uint64_t left = nblk;
+        uint64_t left = nb;
         while (left) {
             const uint32_t chunk = left > 0x40000000ull ? 0x40000000u : (uint32_t)left;
             for (uint32_t bk = 0; bk < chunk; ++bk) {
-                if (match32((uint32_t)w, tlo)) {
+                const uint32_t lo = (uint32_t)w;
+                uint32_t cand = match32<0, DBS>(lo, tlo);
+                if (DBS == 64)
+                    cand |= match32<DBS == 64 ? 32 : 0, DBS>(lo, tlo);
+                if (cand) {
                     uint64_t v = w;
 #pragma unroll 1
-                    for (int j = 0; j < BS; ++j) {
+                    for (int j = 0; j < DBS; ++j) {
                         if (v == wt)
-                            push(job.fb, at0 + (uint64_t)bk * BS + j, p);
+                            push(job.fb, at0 + (uint64_t)bk * DBS + j, p);
                         v = half63(v, p);
                     }
                 }
                 w = redc32(w, plo, phi, pinv32, one);
+                if (DBS == 64)
+                    w = redc32(w, plo, phi, pinv32, one);
             }
-            at0 += (uint64_t)chunk * BS;
+            at0 += (uint64_t)chunk * DBS;
             left -= chunk;
         }
-        for (uint64_t n = s + nblk * BS; n < e; ++n) {  // the short tail, term by term
+        for (uint64_t n = s + nb * DBS; n < e; ++n) {  // the short tail, term by term
             if (w == wt)
                 push(job.fb, n - job.n0, p);
             w = half63(w, p);
-        }    } else if (p < (1ull << 63))
+        }
+    } else if (p < (1ull << 63))
         walk_add63<true>(start(), 0, target, p, s - job.n0, steps, job.fb);
     else
         walk_target(start(), target, p, s - job.n0, steps, job.fb, [p](uint64_t x) { return dblmod(x, p); });
@@ -672,87 +683,7 @@ __device__ __forceinline__ void run_tribonacci(const JobView &job, uint64_t p, u
         return;
     const uint64_t steps = len - 3;  // values T(s+3) .. T(e-1)
     uint64_t i = 0;                   // value T(s+3+i) goes to index idx+3+i
-    if (p < (1ull << 36)) {
-        // The lazily reduced blocks below, with each value held as two
-        // carry-free 32-bit limbs v = h 2^19 + l: from states below 3p < 2^38
-        // (l < 2^19, h < 2^19) twelve steps keep l < 2^31 and h < 2^31, so a
-        // step is one three-input 32-bit add per limb, and the zero test
-        // l p^-1 + h (2^19 p^-1) mod 2^32 < K[j] runs on the multiply pipe.
-        Lazy lz;
-        lz.init(m);
-        constexpr int TB = 12;  // steps per block
-        constexpr uint32_t LOW = (1u << 19) - 1;
-        const uint32_t c19 = lz.pinv32 << 19;  // 2^19 p^-1 mod 2^32
-        uint32_t xl = (uint32_t)x & LOW, xh = (uint32_t)(x >> 19);
-        uint32_t yl = (uint32_t)y & LOW, yh = (uint32_t)(y >> 19);
-        uint32_t zl = (uint32_t)z & LOW, zh = (uint32_t)(z >> 19);
-        uint64_t nb = steps / TB;
-        while (nb) {
-          const uint32_t chunk = nb > 0x40000000ull ? 0x40000000u : (uint32_t)nb;
-          for (uint32_t bk = 0; bk < chunk; ++bk) {
-            uint32_t cand;
-            // operands: %0..%5 = xl, xh, yl, yh, zl, zh, %6 = candidate flag,
-            // %7 = p^-1 mod 2^32, %8 = 2^19 p^-1 mod 2^32
-#define CTD_LZ2_STEP(XL, XH, YL, YH, ZL, ZH, KJ)                                                          \
-    "add.u32 " XL ", " XL ", " YL ";\n\tadd.u32 " XL ", " XL ", " ZL ";\n\t"                            \
-    "add.u32 " XH ", " XH ", " YH ";\n\tadd.u32 " XH ", " XH ", " ZH ";\n\t"                            \
-    "mul.lo.u32 t, " XH ", %8;\n\tmad.lo.u32 t, " XL ", %7, t;\n\tsetp.lt.or.u32 c, t, " #KJ ", c;\n\t"
-#define CTD_LZ2_X(KJ) CTD_LZ2_STEP("%0", "%1", "%2", "%3", "%4", "%5", KJ)
-#define CTD_LZ2_Y(KJ) CTD_LZ2_STEP("%2", "%3", "%4", "%5", "%0", "%1", KJ)
-#define CTD_LZ2_Z(KJ) CTD_LZ2_STEP("%4", "%5", "%0", "%1", "%2", "%3", KJ)
-            asm("{\n\t.reg .pred c;\n\t.reg .b32 t;\n\tsetp.ne.u32 c, %7, %7;\n\t"
-                CTD_LZ2_X(9) CTD_LZ2_Y(15) CTD_LZ2_Z(27) CTD_LZ2_X(51) CTD_LZ2_Y(93) CTD_LZ2_Z(171)
-                CTD_LZ2_X(315) CTD_LZ2_Y(579) CTD_LZ2_Z(1065) CTD_LZ2_X(1959) CTD_LZ2_Y(3603) CTD_LZ2_Z(6627)
-                "selp.u32 %6, 1, 0, c;\n\t}"
-                : "+r"(xl), "+r"(xh), "+r"(yl), "+r"(yh), "+r"(zl), "+r"(zh), "=r"(cand)
-                : "r"(lz.pinv32), "r"(c19));
-#undef CTD_LZ2_X
-#undef CTD_LZ2_Y
-#undef CTD_LZ2_Z
-#undef CTD_LZ2_STEP
-            x = ((uint64_t)xh << 19) + xl;
-            y = ((uint64_t)yh << 19) + yl;
-            z = ((uint64_t)zh << 19) + zl;
-            if (__any_sync(__activemask(), cand)) {  // lanes replay together (see the Fibonacci block)
-                uint64_t a = x, b = y, c = z;  // exact integers: undo the block's TB adds
-#pragma unroll 1
-                for (int j = 0; j < TB; ++j) {
-                    const uint64_t w = c - b - a;
-                    c = b;
-                    b = a;
-                    a = w;
-                }
-                a = lz.full(a);
-                b = lz.full(b);
-                c = lz.full(c);
-                const uint64_t at = idx + 3 + i + (uint64_t)bk * TB;
-#pragma unroll 1
-                for (int j = 0; j < TB; ++j) {
-                    uint64_t w = trib_add(a, b, c, p);
-                    a = b;
-                    b = c;
-                    c = w;
-                    if (w == 0)
-                        push(job.fb, at + j, p);
-                }
-            }
-            x = lz.reduce(x);
-            y = lz.reduce(y);
-            z = lz.reduce(z);
-            xl = (uint32_t)x & LOW;
-            xh = (uint32_t)(x >> 19);
-            yl = (uint32_t)y & LOW;
-            yh = (uint32_t)(y >> 19);
-            zl = (uint32_t)z & LOW;
-            zh = (uint32_t)(z >> 19);
-          }
-          i += (uint64_t)chunk * TB;
-          nb -= chunk;
-        }
-        x = lz.full(((uint64_t)xh << 19) + xl);
-        y = lz.full(((uint64_t)yh << 19) + yl);
-        z = lz.full(((uint64_t)zh << 19) + zl);
-    } else if (p < (1ull << 40)) {
+    if (p < (1ull << 40)) {
         Lazy lz;
         lz.init(m);
         constexpr int TB = 12;  // steps per block
@@ -1087,7 +1018,7 @@ __device__ __forceinline__ void run_peano(const JobView &job, uint64_t p, uint64
 // the others carry block-start copies and reduction constants.
 constexpr int min_ctas_per_sm(uint32_t fam)
 {
-    return fam == PEANO ? 6 : 4;
+    return fam == PEANO ? 6 : ((fam == PROTH || fam == RIESEL || fam == MERSENNE) && DBS == 64 ? 2 : 4);
 }
 
 template <uint32_t FAM>
