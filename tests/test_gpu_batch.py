@@ -93,3 +93,30 @@ def test_served_equals_alone(eng):
     srv.close()
     for k, case in enumerate(MIX):
         assert_same(results[k], case)
+
+
+def test_server_admission_by_memory_budget(eng):
+    """A budget smaller than any job's buffers admits one job at a time (a
+    job that does not fit is still admitted when nothing else runs), and
+    every result equals the oracle's."""
+    srv = ctd.Server(eng, memory_budget=1, max_active=8, segment_length=W)
+    ids = {srv.submit(ctd.CtdJob(f, M, p, n0, n1, f0, f1)): k for k, (f, p, n0, n1, f0, f1) in enumerate(MIX[:4])}
+    results = {}
+    for _ in range(10_000):
+        if len(results) == len(ids):
+            break
+        st = srv.status()
+        assert st["active"] <= 1
+        for jid in srv.tick():
+            results[ids[jid]] = srv.fetch(jid)
+    srv.close()
+    assert len(results) == len(ids)
+    for k in results:
+        assert_same(results[k], MIX[k])
+
+
+def test_batch_rejects_invalid_jobs(eng):
+    jobs, bufs = new_buffers(MIX[:2])
+    jobs[1] = ctd.CtdJob(O.PROTH, M, 0, 1, 10, 3, 100)  # k = 0 is rejected, as by the reference
+    with pytest.raises(ctd.CtdError):
+        eng.batch_run(jobs, bufs)
