@@ -265,6 +265,25 @@ constexpr int BS = 32;
 // per-block overhead per term but need twice the target registers)
 constexpr int DBS = 32;
 
+// Target filter of the doubling families: per thread, two 1024-bit bitmaps in
+// shared memory, each marking a multiplicative hash of the 32 targets' low
+// words.  A block's state passes both with probability ~(32/1024)^2 unless it
+// matches a target, so the 32 exact compares run for about 3% of the warps'
+// blocks instead of every block.  Layout: word k of thread t at
+// [k * blockDim.x + t] (conflict-free: the lanes of a warp hit 32 banks).
+constexpr int FILTER_WORDS = 64;           // two bitmaps of 32 words
+constexpr uint32_t FILTER_A1 = 0x9E3779B1u;  // odd multipliers of the two hashes
+constexpr uint32_t FILTER_A2 = 0x85EBCA77u;
+// blocks a prime needs before building its filter pays off
+constexpr uint64_t FILTER_MIN_BLOCKS = 64;
+extern __shared__ uint32_t ctd_filter_smem[];
+
+template <uint32_t FAM>
+constexpr bool uses_filter()
+{
+    return FAM == PROTH || FAM == RIESEL || FAM == MERSENNE;
+}
+
 // halving mod odd p < 2^63: x/2 or (x + p)/2
 __device__ __forceinline__ uint64_t half63(uint64_t x, uint64_t p) { return (x + ((x & 1) ? p : 0)) >> 1; }
 
@@ -351,6 +370,45 @@ __device__ __forceinline__ void run_doubling(const JobView &job, uint64_t p, uin
         const uint32_t one = (uint32_t)(p & 1);
         uint64_t at0 = s - job.n0;  // index of the current chunk's first term
         uint64_t left = nb;
+        if (DBS == 32 && nb >= FILTER_MIN_BLOCKS) {
+            // blocks through the target filter (see FILTER_WORDS)
+            const uint32_t bd = blockDim.x;
+            uint32_t *const bm = ctd_filter_smem + threadIdx.x;
+#pragma unroll 8
+            for (int k = 0; k < FILTER_WORDS; ++k)
+                bm[k * bd] = 0;
+#pragma unroll 4
+            for (int j = 0; j < DBS; ++j) {
+                const uint32_t h1 = (tlo[j] * FILTER_A1) >> 22, h2 = (tlo[j] * FILTER_A2) >> 22;
+                bm[(h1 >> 5) * bd] |= 1u << (h1 & 31);
+                bm[(32 + (h2 >> 5)) * bd] |= 1u << (h2 & 31);
+            }
+            while (left) {
+                const uint32_t chunk = left > 0x40000000ull ? 0x40000000u : (uint32_t)left;
+                for (uint32_t bk = 0; bk < chunk; ++bk) {
+                    const uint32_t lo = (uint32_t)w;
+                    const uint32_t h1 = (lo * FILTER_A1) >> 22, h2 = (lo * FILTER_A2) >> 22;
+                    const uint32_t f = (bm[(h1 >> 5) * bd] >> (h1 & 31)) & (bm[(32 + (h2 >> 5)) * bd] >> (h2 & 31)) & 1u;
+                    // exact compares and replays are taken by the converged lanes
+                    // together, so the warp never splits
+                    if (__any_sync(__activemask(), f)) {
+                        const uint32_t cand = f ? match32(lo, tlo) : 0u;
+                        if (__any_sync(__activemask(), cand)) {
+                            uint64_t v = w;
+#pragma unroll 1
+                            for (int j = 0; j < DBS; ++j) {
+                                if (v == wt)
+                                    push(job.fb, at0 + (uint64_t)bk * DBS + j, p);
+                                v = half63(v, p);
+                            }
+                        }
+                    }
+                    w = redc32(w, plo, phi, pinv32, one);
+                }
+                at0 += (uint64_t)chunk * DBS;
+                left -= chunk;
+            }
+        }
         while (left) {
             const uint32_t chunk = left > 0x40000000ull ? 0x40000000u : (uint32_t)left;
             for (uint32_t bk = 0; bk < chunk; ++bk) {
@@ -1018,7 +1076,7 @@ __device__ __forceinline__ void run_peano(const JobView &job, uint64_t p, uint64
 // the others carry block-start copies and reduction constants.
 constexpr int min_ctas_per_sm(uint32_t fam)
 {
-    return fam == PEANO ? 6 : ((fam == PROTH || fam == RIESEL || fam == MERSENNE) && DBS == 64 ? 2 : 4);
+    return fam == PEANO ? 6 : ((fam == PROTH || fam == RIESEL || fam == MERSENNE) ? (DBS == 64 ? 2 : 3) : 4);
 }
 
 template <uint32_t FAM>
@@ -1148,11 +1206,31 @@ batch_kernel(const BatchJob *__restrict__ jobs, const uint32_t *__restrict__ act
     }
 }
 
+// dynamic shared memory of a family's kernels at `block` threads
+template <uint32_t FAM>
+constexpr size_t smem_bytes(int block)
+{
+    return uses_filter<FAM>() ? (size_t)FILTER_WORDS * sizeof(uint32_t) * (size_t)block : 0;
+}
+
+// lets a kernel take more than the default 48 KiB of dynamic shared memory
+template <class K>
+static cudaError_t allow_smem(K kernel, size_t bytes)
+{
+    if (bytes <= 48 * 1024)
+        return cudaSuccess;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
 template <uint32_t FAM>
 static cudaError_t launch_batch_fam(const BatchJob *jobs, const uint32_t *active, uint32_t nactive,
                                     const uint64_t *primes, BatchSpan *spans, int grid, cudaStream_t st)
 {
-    batch_kernel<FAM><<<grid, 256, 0, st>>>(jobs, active, nactive, primes, spans);
+    const size_t sm = smem_bytes<FAM>(256);
+    cudaError_t e = allow_smem(batch_kernel<FAM>, sm);
+    if (e != cudaSuccess)
+        return e;
+    batch_kernel<FAM><<<grid, 256, sm, st>>>(jobs, active, nactive, primes, spans);
     return cudaGetLastError();
 }
 
@@ -1200,7 +1278,9 @@ template <uint32_t FAM>
 static int batch_occupancy(int block)
 {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<FAM>, block, 0) != cudaSuccess)
+    const size_t sm = smem_bytes<FAM>(block);
+    if (allow_smem(batch_kernel<FAM>, sm) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<FAM>, block, sm) != cudaSuccess)
         return 0;
     return n;
 }
@@ -1270,7 +1350,11 @@ template <uint32_t FAM>
 static cudaError_t launch_fam(const JobView &v, const uint64_t *d_primes, uint64_t n, int grid, int block,
                               cudaStream_t st)
 {
-    residue_kernel<FAM><<<grid, block, 0, st>>>(v, d_primes, n);
+    const size_t sm = smem_bytes<FAM>(block);
+    cudaError_t e = allow_smem(residue_kernel<FAM>, sm);
+    if (e != cudaSuccess)
+        return e;
+    residue_kernel<FAM><<<grid, block, sm, st>>>(v, d_primes, n);
     return cudaGetLastError();
 }
 
@@ -1305,7 +1389,9 @@ template <uint32_t FAM>
 static int occupancy(int block)
 {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, residue_kernel<FAM>, block, 0) != cudaSuccess)
+    const size_t sm = smem_bytes<FAM>(block);
+    if (allow_smem(residue_kernel<FAM>, sm) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, residue_kernel<FAM>, block, sm) != cudaSuccess)
         return 0;
     return n;
 }
