@@ -265,7 +265,7 @@ constexpr int BS = 32;
 // per-block overhead per term but need twice the target registers)
 constexpr int DBS = 32;
 
-// Target filter of the doubling families: per thread, two 1024-bit bitmaps in
+// Target filter of the baby-step blocks: per thread, two 1024-bit bitmaps in
 // shared memory, each marking a multiplicative hash of the 32 targets' low
 // words.  A block's state passes both with probability ~(32/1024)^2 unless it
 // matches a target, so the 32 exact compares run for about 3% of the warps'
@@ -281,7 +281,33 @@ extern __shared__ uint32_t ctd_filter_smem[];
 template <uint32_t FAM>
 constexpr bool uses_filter()
 {
-    return FAM == PROTH || FAM == RIESEL || FAM == MERSENNE;
+    return FAM == PROTH || FAM == RIESEL || FAM == MERSENNE || FAM == PROTH_FIXED_N || FAM == RIESEL_FIXED_N;
+}
+
+// this thread's filter column
+__device__ __forceinline__ uint32_t *filter_column() { return ctd_filter_smem + threadIdx.x; }
+
+// builds the filter of the 32 targets' low words
+__device__ __forceinline__ void filter_build(uint32_t *bm, const uint32_t (&tlo)[32])
+{
+    const uint32_t bd = blockDim.x;
+#pragma unroll 8
+    for (int k = 0; k < FILTER_WORDS; ++k)
+        bm[k * bd] = 0;
+#pragma unroll 4
+    for (int j = 0; j < 32; ++j) {
+        const uint32_t h1 = (tlo[j] * FILTER_A1) >> 22, h2 = (tlo[j] * FILTER_A2) >> 22;
+        bm[(h1 >> 5) * bd] |= 1u << (h1 & 31);
+        bm[(32 + (h2 >> 5)) * bd] |= 1u << (h2 & 31);
+    }
+}
+
+// 1 if lo may equal one of the targets (always when it does)
+__device__ __forceinline__ uint32_t filter_pass(const uint32_t *bm, uint32_t lo)
+{
+    const uint32_t bd = blockDim.x;
+    const uint32_t h1 = (lo * FILTER_A1) >> 22, h2 = (lo * FILTER_A2) >> 22;
+    return (bm[(h1 >> 5) * bd] >> (h1 & 31)) & (bm[(32 + (h2 >> 5)) * bd] >> (h2 & 31)) & 1u;
 }
 
 // halving mod odd p < 2^63: x/2 or (x + p)/2
@@ -372,23 +398,13 @@ __device__ __forceinline__ void run_doubling(const JobView &job, uint64_t p, uin
         uint64_t left = nb;
         if (DBS == 32 && nb >= FILTER_MIN_BLOCKS) {
             // blocks through the target filter (see FILTER_WORDS)
-            const uint32_t bd = blockDim.x;
-            uint32_t *const bm = ctd_filter_smem + threadIdx.x;
-#pragma unroll 8
-            for (int k = 0; k < FILTER_WORDS; ++k)
-                bm[k * bd] = 0;
-#pragma unroll 4
-            for (int j = 0; j < DBS; ++j) {
-                const uint32_t h1 = (tlo[j] * FILTER_A1) >> 22, h2 = (tlo[j] * FILTER_A2) >> 22;
-                bm[(h1 >> 5) * bd] |= 1u << (h1 & 31);
-                bm[(32 + (h2 >> 5)) * bd] |= 1u << (h2 & 31);
-            }
+            uint32_t *const bm = filter_column();
+            filter_build(bm, tlo);
             while (left) {
                 const uint32_t chunk = left > 0x40000000ull ? 0x40000000u : (uint32_t)left;
                 for (uint32_t bk = 0; bk < chunk; ++bk) {
                     const uint32_t lo = (uint32_t)w;
-                    const uint32_t h1 = (lo * FILTER_A1) >> 22, h2 = (lo * FILTER_A2) >> 22;
-                    const uint32_t f = (bm[(h1 >> 5) * bd] >> (h1 & 31)) & (bm[(32 + (h2 >> 5)) * bd] >> (h2 & 31)) & 1u;
+                    const uint32_t f = filter_pass(bm, lo);
                     // exact compares and replays are taken by the converged lanes
                     // together, so the warp never splits
                     if (__any_sync(__activemask(), f)) {
@@ -472,6 +488,34 @@ __device__ __forceinline__ void run_fixed_n(const JobView &job, uint64_t p, uint
         uint64_t vb = v;
         uint64_t at0 = s - job.n0;  // index of the current chunk's first term
         uint64_t left = nblk;
+        if (nblk >= FILTER_MIN_BLOCKS) {
+            // blocks through the target filter, as for the doubling families
+            uint32_t *const bm = filter_column();
+            filter_build(bm, tlo);
+            while (left) {
+                const uint32_t chunk = left > 0x40000000ull ? 0x40000000u : (uint32_t)left;
+                for (uint32_t bk = 0; bk < chunk; ++bk) {
+                    const uint32_t lo = (uint32_t)vb;
+                    const uint32_t f = filter_pass(bm, lo);
+                    if (__any_sync(__activemask(), f)) {
+                        const uint32_t cand = f ? match32(lo, tlo) : 0u;
+                        if (__any_sync(__activemask(), cand)) {
+                            const uint64_t tgt = (FAM == PROTH_FIXED_N) ? p - 1 : 1;
+                            uint64_t x = vb;
+#pragma unroll 1
+                            for (int j = 0; j < BS; ++j) {
+                                if (x == tgt)
+                                    push(job.fb, at0 + (uint64_t)bk * BS + j, p);
+                                x = add63(x, c, p);
+                            }
+                        }
+                    }
+                    vb = add63(vb, W, p);
+                }
+                at0 += (uint64_t)chunk * BS;
+                left -= chunk;
+            }
+        }
         while (left) {
             const uint32_t chunk = left > 0x40000000ull ? 0x40000000u : (uint32_t)left;
             for (uint32_t bk = 0; bk < chunk; ++bk) {
@@ -1076,7 +1120,8 @@ __device__ __forceinline__ void run_peano(const JobView &job, uint64_t p, uint64
 // the others carry block-start copies and reduction constants.
 constexpr int min_ctas_per_sm(uint32_t fam)
 {
-    return fam == PEANO ? 6 : ((fam == PROTH || fam == RIESEL || fam == MERSENNE) ? (DBS == 64 ? 2 : 3) : 4);
+    return fam == PEANO ? 6 : ((fam == PROTH || fam == RIESEL || fam == MERSENNE) ? (DBS == 64 ? 2 : 3)
+                                : (fam == PROTH_FIXED_N || fam == RIESEL_FIXED_N) ? 3 : 4);
 }
 
 template <uint32_t FAM>
