@@ -261,22 +261,24 @@ struct Lazy {
 // runs on the multiply pipe.  A block whose low words matched is replayed
 // term by term with the full test, so results are those of the walk.
 constexpr int BS = 32;
-// terms per block of the doubling families (32 or 64: 64 targets halve the
-// per-block overhead per term but need twice the target registers)
-constexpr int DBS = 32;
 
-// Target filter of the baby-step blocks: per thread, two 1024-bit bitmaps in
-// shared memory, each marking a multiplicative hash of the 32 targets' low
-// words.  A block's state passes both with probability ~(32/1024)^2 unless it
-// matches a target, so the 32 exact compares run for about 3% of the warps'
-// blocks instead of every block.  Layout: word k of thread t at
-// [k * blockDim.x + t] (conflict-free: the lanes of a warp hit 32 banks).
-constexpr int FILTER_WORDS = 64;           // two bitmaps of 32 words
-constexpr uint32_t FILTER_A1 = 0x9E3779B1u;  // odd multipliers of the two hashes
-constexpr uint32_t FILTER_A2 = 0x85EBCA77u;
+// Target filter of the baby-step blocks: per thread, 32 slots of two 32-bit
+// words in shared memory.  A target's low word t is hashed once, h = t *
+// FILTER_A; slot h >> 27 gets bit t mod 32 set in its first word and bit
+// (h >> 22) mod 32 in its second.  A state whose low word equals a target
+// always passes (both bits set); any other passes with probability about
+// E[X^2]/32^2 = 2/1024 for the X ~ Poisson(1) targets in its slot, so the
+// exact compares run for about 5 % of the warps' blocks.  A test is one
+// 64-bit load and two funnel-shift bit tests (the funnel shift takes its
+// amount mod 32, so no masking).  Layout: slot k of thread t at [k *
+// blockDim.x + t] (conflict-free: the lanes of a warp read consecutive
+// slots).
+constexpr int FILTER_WORDS = 64;  // 32-bit words per thread
+constexpr int FILTER_SLOTS = FILTER_WORDS / 2;
+constexpr uint32_t FILTER_A = 0x9E3779B1u;  // odd multiplier of the hash
 // blocks a prime needs before building its filter pays off
-constexpr uint64_t FILTER_MIN_BLOCKS = 64;
-extern __shared__ uint32_t ctd_filter_smem[];
+constexpr uint64_t FILTER_MIN_BLOCKS = 16;
+extern __shared__ __align__(16) uint32_t ctd_filter_smem[];
 
 template <uint32_t FAM>
 constexpr bool uses_filter()
@@ -284,31 +286,41 @@ constexpr bool uses_filter()
     return FAM == PROTH || FAM == RIESEL || FAM == MERSENNE || FAM == PROTH_FIXED_N || FAM == RIESEL_FIXED_N;
 }
 
-// this thread's filter column
-__device__ __forceinline__ uint32_t *filter_column() { return ctd_filter_smem + threadIdx.x; }
+struct TargetFilter {
+    uint2 *col;       // this thread's slot 0
+    uint32_t stride;  // slots between a thread's consecutive slots
 
-// builds the filter of the 32 targets' low words
-__device__ __forceinline__ void filter_build(uint32_t *bm, const uint32_t (&tlo)[32])
-{
-    const uint32_t bd = blockDim.x;
-#pragma unroll 8
-    for (int k = 0; k < FILTER_WORDS; ++k)
-        bm[k * bd] = 0;
-#pragma unroll 4
-    for (int j = 0; j < 32; ++j) {
-        const uint32_t h1 = (tlo[j] * FILTER_A1) >> 22, h2 = (tlo[j] * FILTER_A2) >> 22;
-        bm[(h1 >> 5) * bd] |= 1u << (h1 & 31);
-        bm[(32 + (h2 >> 5)) * bd] |= 1u << (h2 & 31);
+    __device__ __forceinline__ TargetFilter()
+        : col(reinterpret_cast<uint2 *>(ctd_filter_smem) + threadIdx.x), stride(blockDim.x)
+    {
     }
-}
 
-// 1 if lo may equal one of the targets (always when it does)
-__device__ __forceinline__ uint32_t filter_pass(const uint32_t *bm, uint32_t lo)
-{
-    const uint32_t bd = blockDim.x;
-    const uint32_t h1 = (lo * FILTER_A1) >> 22, h2 = (lo * FILTER_A2) >> 22;
-    return (bm[(h1 >> 5) * bd] >> (h1 & 31)) & (bm[(32 + (h2 >> 5)) * bd] >> (h2 & 31)) & 1u;
-}
+    __device__ __forceinline__ uint2 &slot(uint32_t h) const { return col[(h >> 27) * stride]; }
+
+    // marks the 32 targets' low words
+    __device__ __forceinline__ void build(const uint32_t (&tlo)[BS]) const
+    {
+#pragma unroll 8
+        for (int k = 0; k < FILTER_SLOTS; ++k)
+            col[k * stride] = uint2{0, 0};
+#pragma unroll 4
+        for (int j = 0; j < BS; ++j) {
+            const uint32_t t = tlo[j], h = t * FILTER_A;
+            uint2 &sl = slot(h);
+            sl.x |= 1u << (t & 31);
+            sl.y |= 1u << ((h >> 22) & 31);
+        }
+    }
+
+    // bit 0 set if lo may equal one of the targets (always when it does);
+    // the other bits are arbitrary
+    __device__ __forceinline__ uint32_t test(uint32_t lo) const
+    {
+        const uint32_t h = lo * FILTER_A;
+        const uint2 sl = slot(h);
+        return __funnelshift_r(sl.x, sl.x, lo) & __funnelshift_r(sl.y, sl.y, h >> 22);
+    }
+};
 
 // halving mod odd p < 2^63: x/2 or (x + p)/2
 __device__ __forceinline__ uint64_t half63(uint64_t x, uint64_t p) { return (x + ((x & 1) ? p : 0)) >> 1; }
@@ -338,6 +350,90 @@ __device__ __forceinline__ uint32_t match32(uint32_t lo, const uint32_t (&t)[N])
     return f;
 }
 #undef CTD_M4
+
+// nb blocks of BS terms from state x, block numbers b0, b0 + 1, ..., with
+// the 32 compares of every block and lane-wise replays of the rare matches;
+// returns the state after them.  step(x) is the giant step to the next
+// block's state; replay(x, b) re-walks block b term by term with the full
+// test.
+template <typename Step, typename Replay>
+__device__ __forceinline__ uint64_t plain_blocks(const uint32_t (&tlo)[BS], uint64_t x, uint64_t b0, uint64_t nb,
+                                                 Step step, Replay replay)
+{
+    for (uint64_t done = 0; done < nb;) {
+        const uint32_t chunk = nb - done > 0x40000000ull ? 0x40000000u : (uint32_t)(nb - done);
+        for (uint32_t bk = 0; bk < chunk; ++bk) {
+            if (match32((uint32_t)x, tlo))
+                replay(x, b0 + done + bk);
+            x = step(x);
+        }
+        done += chunk;
+    }
+    return x;
+}
+
+// ng groups of FILTER_GROUP blocks from state x through the target filter,
+// one warp vote a group; returns the state after them.  In a group with a
+// passing lane, the blocks some lane passed get the exact compares (lanes
+// that passed) and, on a match, the replay (all lanes together, so the warp
+// never splits).  That path keeps only the group's first state and steps
+// from it, so little stays live across the loop (the targets fill 32
+// registers) and its code exists once.
+constexpr int FILTER_GROUP = 4;
+template <typename Step, typename Replay>
+__device__ __forceinline__ uint64_t filtered_groups(const uint32_t (&tlo)[BS], uint64_t x, uint64_t ng, Step step,
+                                                    Replay replay)
+{
+    const TargetFilter flt;
+    flt.build(tlo);
+    for (uint64_t done = 0; done < ng;) {
+        const uint32_t chunk = ng - done > 0x10000000ull ? 0x10000000u : (uint32_t)(ng - done);
+        for (uint32_t g = 0; g < chunk; ++g) {
+            const uint64_t x0 = x;
+            uint32_t fs[FILTER_GROUP], any = 0;
+#pragma unroll
+            for (int i = 0; i < FILTER_GROUP; ++i) {
+                fs[i] = flt.test((uint32_t)x) & 1;
+                any |= fs[i];
+                x = step(x);
+            }
+            if (__any_sync(__activemask(), any)) {
+                const uint32_t act = __activemask();
+                uint32_t pass = 0;
+#pragma unroll
+                for (int i = 0; i < FILTER_GROUP; ++i)
+                    pass |= fs[i] << i;
+                // the blocks some lane passed, lowest first (warp-uniform)
+                uint64_t z = x0;
+                int at = 0;
+                for (uint32_t todo = __reduce_or_sync(act, pass); todo; todo &= todo - 1) {
+                    const int i = __ffs(todo) - 1;
+                    for (; at < i; ++at)
+                        z = step(z);
+                    const uint32_t cand = (pass >> i) & 1 ? match32((uint32_t)z, tlo) : 0u;
+                    if (__any_sync(act, cand))
+                        replay(z, (done + g) * FILTER_GROUP + i);
+                }
+            }
+        }
+        done += chunk;
+    }
+    return x;
+}
+
+// the blocks of a range: filtered when it is long enough to pay for the
+// filter (the last nb mod FILTER_GROUP blocks unfiltered)
+template <typename Step, typename Replay>
+__device__ __forceinline__ uint64_t run_blocks(const uint32_t (&tlo)[BS], uint64_t x, uint64_t nb, Step step,
+                                               Replay replay)
+{
+    uint64_t b0 = 0;
+    if (nb >= FILTER_MIN_BLOCKS) {
+        x = filtered_groups(tlo, x, nb / FILTER_GROUP, step, replay);
+        b0 = nb - nb % FILTER_GROUP;
+    }
+    return plain_blocks(tlo, x, b0, nb - b0, step, replay);
+}
 
 // u * 2^-32 mod p for u < p, odd p < 2^63: one 32-bit Montgomery reduction,
 // m = u_lo (-p^-1) mod 2^32, r = (u + m p) / 2^32.  u + m p = 0 mod 2^32 and
@@ -375,7 +471,7 @@ __device__ __forceinline__ void run_doubling(const JobView &job, uint64_t p, uin
         const uint64_t k = job.param < p ? job.param : job.param % p;
         return m.mul(U, k);
     };
-    if (p < (1ull << 63) && (e - s) / DBS >= 2 && job.variant != CTD_VARIANT_WALK) {
+    if (p < (1ull << 63) && (e - s) / BS >= 2 && job.variant != CTD_VARIANT_WALK) {
         // Walk w(n) = 2^-n instead: k 2^n = -1 (Proth) / 1 (Riesel, Mersenne
         // with k = 1) mod p iff w(n) = -k / k, a fixed target, and the giant
         // step w -> w 2^-32 is one reduction on the multiply pipe (redc32).
@@ -384,71 +480,28 @@ __device__ __forceinline__ void run_doubling(const JobView &job, uint64_t p, uin
         const uint64_t wt = (FAM == PROTH) ? (k ? p - k : 0) : k;  // target of w
         const uint64_t sr = s < p - 1 ? s : s % (p - 1);
         uint64_t w = m.from(m.pow2(p - 1 - sr));  // 2^-s mod p (Fermat)
-        const uint64_t nb = (e - s) / DBS;
-        uint32_t tlo[DBS];
+        const uint64_t nb = (e - s) / BS;
+        uint32_t tlo[BS];
         uint64_t t = wt;
 #pragma unroll
-        for (int j = 0; j < DBS; ++j) {
+        for (int j = 0; j < BS; ++j) {
             tlo[j] = (uint32_t)t;
             t = add63(t, t, p);
         }
         const uint32_t plo = (uint32_t)p, phi = (uint32_t)(p >> 32), pinv32 = (uint32_t)m.pinv;
         const uint32_t one = (uint32_t)(p & 1);
-        uint64_t at0 = s - job.n0;  // index of the current chunk's first term
-        uint64_t left = nb;
-        if (DBS == 32 && nb >= FILTER_MIN_BLOCKS) {
-            // blocks through the target filter (see FILTER_WORDS)
-            uint32_t *const bm = filter_column();
-            filter_build(bm, tlo);
-            while (left) {
-                const uint32_t chunk = left > 0x40000000ull ? 0x40000000u : (uint32_t)left;
-                for (uint32_t bk = 0; bk < chunk; ++bk) {
-                    const uint32_t lo = (uint32_t)w;
-                    const uint32_t f = filter_pass(bm, lo);
-                    // exact compares and replays are taken by the converged lanes
-                    // together, so the warp never splits
-                    if (__any_sync(__activemask(), f)) {
-                        const uint32_t cand = f ? match32(lo, tlo) : 0u;
-                        if (__any_sync(__activemask(), cand)) {
-                            uint64_t v = w;
+        const uint64_t at0 = s - job.n0;  // index of the first term
+        auto giant = [&](uint64_t x) { return redc32(x, plo, phi, pinv32, one); };
+        auto replay = [&](uint64_t v, uint64_t b) {
 #pragma unroll 1
-                            for (int j = 0; j < DBS; ++j) {
-                                if (v == wt)
-                                    push(job.fb, at0 + (uint64_t)bk * DBS + j, p);
-                                v = half63(v, p);
-                            }
-                        }
-                    }
-                    w = redc32(w, plo, phi, pinv32, one);
-                }
-                at0 += (uint64_t)chunk * DBS;
-                left -= chunk;
+            for (int j = 0; j < BS; ++j) {
+                if (v == wt)
+                    push(job.fb, at0 + b * BS + j, p);
+                v = half63(v, p);
             }
-        }
-        while (left) {
-            const uint32_t chunk = left > 0x40000000ull ? 0x40000000u : (uint32_t)left;
-            for (uint32_t bk = 0; bk < chunk; ++bk) {
-                const uint32_t lo = (uint32_t)w;
-                uint32_t cand = match32<0, DBS>(lo, tlo);
-                if (DBS == 64)
-                    cand |= match32<DBS == 64 ? 32 : 0, DBS>(lo, tlo);
-                if (cand) {
-                    uint64_t v = w;
-#pragma unroll 1
-                    for (int j = 0; j < DBS; ++j) {
-                        if (v == wt)
-                            push(job.fb, at0 + (uint64_t)bk * DBS + j, p);
-                        v = half63(v, p);
-                    }
-                }
-                w = redc32(w, plo, phi, pinv32, one);
-                if (DBS == 64)
-                    w = redc32(w, plo, phi, pinv32, one);
-            }
-            at0 += (uint64_t)chunk * DBS;
-            left -= chunk;
-        }
-        for (uint64_t n = s + nb * DBS; n < e; ++n) {  // the short tail, term by term
+        };
+        w = run_blocks(tlo, w, nb, giant, replay);
+        for (uint64_t n = s + nb * BS; n < e; ++n) {  // the short tail, term by term
             if (w == wt)
                 push(job.fb, n - job.n0, p);
             w = half63(w, p);
@@ -485,55 +538,17 @@ __device__ __forceinline__ void run_fixed_n(const JobView &job, uint64_t p, uint
 #pragma unroll
         for (int j = 0; j < 5; ++j)  // BS c = 2^5 c
             W = dblmod(W, p);
-        uint64_t vb = v;
-        uint64_t at0 = s - job.n0;  // index of the current chunk's first term
-        uint64_t left = nblk;
-        if (nblk >= FILTER_MIN_BLOCKS) {
-            // blocks through the target filter, as for the doubling families
-            uint32_t *const bm = filter_column();
-            filter_build(bm, tlo);
-            while (left) {
-                const uint32_t chunk = left > 0x40000000ull ? 0x40000000u : (uint32_t)left;
-                for (uint32_t bk = 0; bk < chunk; ++bk) {
-                    const uint32_t lo = (uint32_t)vb;
-                    const uint32_t f = filter_pass(bm, lo);
-                    if (__any_sync(__activemask(), f)) {
-                        const uint32_t cand = f ? match32(lo, tlo) : 0u;
-                        if (__any_sync(__activemask(), cand)) {
-                            const uint64_t tgt = (FAM == PROTH_FIXED_N) ? p - 1 : 1;
-                            uint64_t x = vb;
+        const uint64_t at0 = s - job.n0;  // index of the first term
+        auto giant = [&](uint64_t x) { return add63(x, W, p); };
+        auto replay = [&](uint64_t x, uint64_t b) {
 #pragma unroll 1
-                            for (int j = 0; j < BS; ++j) {
-                                if (x == tgt)
-                                    push(job.fb, at0 + (uint64_t)bk * BS + j, p);
-                                x = add63(x, c, p);
-                            }
-                        }
-                    }
-                    vb = add63(vb, W, p);
-                }
-                at0 += (uint64_t)chunk * BS;
-                left -= chunk;
+            for (int j = 0; j < BS; ++j) {
+                if (x == target)
+                    push(job.fb, at0 + b * BS + j, p);
+                x = add63(x, c, p);
             }
-        }
-        while (left) {
-            const uint32_t chunk = left > 0x40000000ull ? 0x40000000u : (uint32_t)left;
-            for (uint32_t bk = 0; bk < chunk; ++bk) {
-                if (match32((uint32_t)vb, tlo)) {
-                    const uint64_t tgt = (FAM == PROTH_FIXED_N) ? p - 1 : 1;
-                    uint64_t x = vb;
-#pragma unroll 1
-                    for (int j = 0; j < BS; ++j) {
-                        if (x == tgt)
-                            push(job.fb, at0 + (uint64_t)bk * BS + j, p);
-                        x = add63(x, c, p);
-                    }
-                }
-                vb = add63(vb, W, p);
-            }
-            at0 += (uint64_t)chunk * BS;
-            left -= chunk;
-        }
+        };
+        const uint64_t vb = run_blocks(tlo, v, nblk, giant, replay);
         const uint64_t ts = s + nblk * BS;
         if (ts < e)
             walk_add63<false>(vb, c, target, p, ts - job.n0, e - ts - 1, job.fb);
@@ -1120,8 +1135,9 @@ __device__ __forceinline__ void run_peano(const JobView &job, uint64_t p, uint64
 // the others carry block-start copies and reduction constants.
 constexpr int min_ctas_per_sm(uint32_t fam)
 {
-    return fam == PEANO ? 6 : ((fam == PROTH || fam == RIESEL || fam == MERSENNE) ? (DBS == 64 ? 2 : 3)
-                                : (fam == PROTH_FIXED_N || fam == RIESEL_FIXED_N) ? 3 : 4);
+    return fam == PEANO ? 6
+                        : (fam == PROTH || fam == RIESEL || fam == MERSENNE || fam == PROTH_FIXED_N || fam == RIESEL_FIXED_N) ? 3
+                                                                                                                   : 4;
 }
 
 template <uint32_t FAM>
