@@ -80,12 +80,12 @@ FAMILY_NAMES = {0: "MERSENNE", 1: "PROTH", 2: "RIESEL", 3: "SMARANDACHE", 4: "FI
 # exact algorithm the kernel runs; multiplies, which go to the multiply pipe,
 # are listed separately):
 #  * doubling (Proth/Riesel/Mersenne): baby-step/giant-step blocks of 32
-#    terms through a per-prime target filter: per block two hash shifts, two
-#    word-index shifts, two bit extracts, one AND and the test (8), the 32
-#    exact compares on the ~3% of blocks a warp's filter passes (~1); the
-#    giant step (a 32-bit Montgomery reduction) is on the multiply pipe
-#    -> 9/32;
-#  * fixed-n: the same filtered blocks, giant step a modular add (5) -> 14/32;
+#    terms through a per-prime target filter: per block a slot shift, a field
+#    shift, two funnel-shift bit tests, their AND and the OR into the vote of
+#    a group of four blocks (6), the 32 exact compares on the ~5.5% of
+#    warp-blocks some lane passes (~2); the giant step (a 32-bit Montgomery
+#    reduction) and the hash multiply are on the multiply pipe -> 8/32;
+#  * fixed-n: the same filtered blocks, giant step a modular add (5) -> 13/32;
 #  * Fibonacci/Lucas (p < 2^40): lazily reduced blocks of 16 steps: a 64-bit
 #    add (2) and the zero-test compare (1) per step, plus one shift per state
 #    for the block-end reduction (2 per 16 steps) -> 3.125; the test's
@@ -94,7 +94,7 @@ FAMILY_NAMES = {0: "MERSENNE", 1: "PROTH", 2: "RIESEL", 3: "SMARANDACHE", 4: "FI
 #    and the compare (1) per step, 3 shifts per block -> 3.25;
 #  * Smarandache (64-bit Shoup): adds/subtracts of x M + m - q p (4) and
 #    two low-word compares = 6, plus 9 32-bit multiplies.
-ALU_OPS_PER_UPDATE = {0: 9 / 32, 1: 9 / 32, 2: 9 / 32, 6: 14 / 32, 7: 14 / 32, 4: 50 / 16, 5: 50 / 16, 8: 39 / 12,
+ALU_OPS_PER_UPDATE = {0: 8 / 32, 1: 8 / 32, 2: 8 / 32, 6: 13 / 32, 7: 13 / 32, 4: 50 / 16, 5: 50 / 16, 8: 39 / 12,
                       3: 6}
 # DRAM bytes per prime of residue_kernel<PROTH> from one ncu capture on
 # [2^32, 2^32 + 2^27): 48,436,480 + 1,024 bytes for 6,047,768 primes; each
