@@ -372,6 +372,7 @@ int ctd_serve_tick(ctd_server *srv, uint64_t *done_ids, uint32_t cap, uint32_t *
         CTX_TRY(cudaMallocAsync(&q.d_counts, N * sizeof(uint32_t), st));
         CTX_TRY(cudaMallocAsync(&q.d_factors, N * q.job.max_factors * sizeof(uint64_t), st));
         CTX_TRY(cudaMemsetAsync(q.d_counts, 0, N * sizeof(uint32_t), st));
+        CTX_TRY(cudaMemsetAsync(q.d_factors, 0, N * q.job.max_factors * sizeof(uint64_t), st));
         if (q.job.f0 <= 2 && q.job.f1 > 2) {
             int rc = launch_mod2(view_of(ctx, q.job, q.d_counts, q.d_factors), st, err);
             if (rc)

@@ -264,6 +264,15 @@ int ctd_open(int device, ctd_ctx **out)
         delete ctx;
         return code;
     }
+    // device tables of the residue kernels, uploaded before any launch or
+    // graph capture on this device
+    std::string terr;
+    const int trc = prepare_residue_tables(device, terr);
+    if (trc != CTD_OK) {
+        cudaStreamDestroy(ctx->stream);
+        delete ctx;
+        return trc;
+    }
     ctx->ws = sieve_workspace_create();
     *out = ctx;
     return CTD_OK;

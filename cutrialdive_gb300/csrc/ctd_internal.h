@@ -95,6 +95,10 @@ int sieve_range_scratch(const SieveScratch &sc, int sm_count, uint64_t lo, uint6
                         uint64_t capacity, uint64_t *count, cudaStream_t stream, std::string &err);
 
 // -------------------------------------------------------------- residues
+// Uploads the residue kernels' per-device tables (the trial-division primes
+// of the Fibonacci/Lucas rank-of-apparition path) to `device`, the current
+// device, once per process and device.
+int prepare_residue_tables(int device, std::string &err);
 // Odd primes only.  Launches the family's residue kernel over
 // nprimes x view.tiles work items.
 int launch_residues(const JobView &view, const uint64_t *d_primes, uint64_t nprimes, int grid, int block,

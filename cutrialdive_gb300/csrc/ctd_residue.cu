@@ -19,6 +19,8 @@
 #include "ctd_internal.h"
 
 #include <atomic>
+#include <mutex>
+#include <vector>
 
 namespace ctd {
 
@@ -30,14 +32,62 @@ void note_kernel_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); 
 uint64_t kernel_launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 // ----------------------------------------------------------------- push
+// Keeps a term's max_factors smallest primes once more primes than slots
+// divide it.  Called together by the lanes `peers` pushing to the same
+// term; `pending` lanes still hold a prime without a slot.  Each round the
+// leader finds the largest value in the slots (an empty slot, 0, counts as
+// larger than any prime); every pending lane whose prime is not below it
+// gives up (values only decrease, so it never will be), and the lowest
+// remaining lane replaces that value with its prime by an exchange.  Each
+// successful exchange replaces the current largest value by a smaller one,
+// so after all pushes the slots hold the smallest primes pushed, whatever
+// their order -- the set of the reference's CPU engine, which walks the
+// primes in ascending order.  A failed exchange (another push changed the
+// slots) leaves the lane pending; the rounds are bounded.
+__device__ __forceinline__ void push_overflow(unsigned long long *slots, uint32_t k, unsigned long long p, bool pending,
+                                           uint32_t peers, int leader)
+{
+    const int lane = (int)(threadIdx.x & 31u);
+    for (int round = 0; round < (1 << 16); ++round) {
+        if (!__any_sync(peers, pending))
+            return;
+        unsigned long long m = 0, raw = 0;
+        uint32_t j = 0;
+        if (lane == leader) {
+            for (uint32_t i = 0; i < k; ++i) {
+                const unsigned long long v = *(volatile unsigned long long *)&slots[i];
+                const unsigned long long key = v ? v : ~0ull;
+                if (key > m) {
+                    m = key;
+                    raw = v;
+                    j = i;
+                    if (!v)
+                        break;
+                }
+            }
+        }
+        m = __shfl_sync(peers, m, leader);
+        raw = __shfl_sync(peers, raw, leader);
+        j = __shfl_sync(peers, j, leader);
+        if (pending && p >= m)
+            pending = false;
+        const uint32_t want = __ballot_sync(peers, pending);
+        if (want && lane == __ffs(want) - 1 && atomicCAS(&slots[j], raw, p) == raw)
+            pending = false;
+    }
+}
+
 // factors_buffer push (src/device_factors_buffer.hpp:119-129): atomic slot
-// reservation, store only below the per-term capacity; the count keeps
-// growing so overflow is visible to the host.  Warp-aggregated: the lanes
-// that push to the same term at the same time (every prime divides a zero
-// term such as T(1)) are grouped with a match, their leader reserves all
-// their slots with one atomic, and each lane stores at its rank -- one
-// atomic per (warp, term) instead of one per lane.  Slot order stays the
-// order of reservation, as in the reference.
+// reservation; the count keeps growing past the per-term capacity so the
+// excess is visible to the host.  Beyond the capacity the reference's device
+// push drops whatever arrives late; here the term keeps its smallest primes
+// (push_overflow), which is deterministic and equals the CPU engine's
+// result.  Warp-aggregated: the lanes that push to the same term at the same
+// time (every prime divides a zero term such as T(1)) are grouped with a
+// match, their leader reserves all their slots with one atomic, and each
+// lane takes the slot of its rank -- one atomic per (warp, term) instead of
+// one per lane; past the capacity the group shares push_overflow's scans.
+// Slots past a term's count must be zero on entry.
 __device__ __forceinline__ void push(const FactorsView &fb, uint64_t idx, uint64_t p)
 {
     const uint32_t active = __activemask();
@@ -49,8 +99,12 @@ __device__ __forceinline__ void push(const FactorsView &fb, uint64_t idx, uint64
         base = atomicAdd(&fb.counts[idx], (uint32_t)__popc(peers));
     base = __shfl_sync(peers, base, leader);
     const uint32_t pos = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
-    if (pos < fb.max_factors)
-        fb.factors[idx * fb.max_factors + pos] = p;
+    unsigned long long *const slots = (unsigned long long *)(fb.factors + idx * fb.max_factors);
+    // the reserved slot, unless a push beyond the term's capacity took it
+    // first; beyond capacity, the term keeps its smallest primes
+    const bool pending = !(pos < fb.max_factors && atomicCAS(&slots[pos], 0ull, (unsigned long long)p) == 0ull);
+    if (__builtin_expect(__any_sync(peers, pending), 0))
+        push_overflow(slots, fb.max_factors, p, pending, peers, leader);
 }
 
 // ------------------------------------------------------- step primitives
@@ -578,6 +632,136 @@ __device__ __forceinline__ void fib_pair(const Mont &m, uint64_t k, uint64_t &fk
     fk1 = b;
 }
 
+// Odd primes below 2^20 for the trial division of the rank-of-apparition
+// path, one 16-byte entry each: {q^-1 mod 2^64 (low, high word), high word
+// of floor((2^64 - 1) / q), q}.  x = R q^-1 mod 2^64 equals R / q when q | R,
+// which holds iff x q < 2^64; a high word of x above the bound's rules that
+// out with one compare.  Filled once per device by prepare_residue_tables.
+constexpr uint32_t TRIAL_LIMIT = 1u << 20;
+constexpr uint32_t TRIAL_PRIMES = 82024;  // odd primes below 2^20
+__device__ uint4 g_trial_div[TRIAL_PRIMES];
+
+// number of table primes <= b (b < TRIAL_LIMIT)
+__device__ __forceinline__ uint32_t trial_count(uint64_t b)
+{
+    uint32_t lo = 0, hi = TRIAL_PRIMES;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (g_trial_div[mid].w <= b)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// Fibonacci / Lucas by the rank of apparition.  For a prime p other than 2
+// and 5, p | F(n) iff a(p) | n, where a(p), the rank of apparition, divides
+// D = p - (5/p) (Legendre symbol: +1 for p = +-1 mod 5, -1 for p = +-2);
+// p | L(n) iff a(p) is even and n is an odd multiple of a(p)/2 (L(n) =
+// F(2n)/F(n) and gcd(F(n), L(n)) | 2).  Hits in [s, e) need a(p) <= 2(e - 1),
+// so every odd prime factor of a(p) is at most e - 1 (for Lucas it divides
+// a(p)/2 <= e - 1): a(p) then divides S, the part of D built from 2 and the
+// primes up to e - 1, found by trial division.  F(S) = 0 mod p tells whether
+// it does; if so, a(p) is S reduced prime by prime while F stays zero.  The
+// pushed (n, p) pairs are exactly those of the walk.  Needs s >= 1, odd
+// p != 5 below 2^63 and e - 1 < TRIAL_LIMIT.
+template <uint32_t FAM>
+__device__ void run_fibonacci_rank(const JobView &job, uint64_t p, uint64_t s, uint64_t e)
+{
+    const uint64_t r5 = p % 5;
+    const uint64_t D = (r5 == 1 || r5 == 4) ? p - 1 : p + 1;
+    const uint64_t bmax = e - 1;  // largest prime factor that can matter
+    const int v2 = __ffsll((long long)D) - 1;
+    uint64_t R = D >> v2;  // part of D not yet factored
+    uint64_t S = 1ull << v2;
+    uint32_t fq[16], fv[16];
+    int nf = 0;
+    const uint32_t nq = trial_count(bmax);
+    const uint4 *__restrict__ tab = g_trial_div;
+    uint32_t i = 0;
+    // 64 primes at a time; between rounds, stop once q^2 > R (R is then 1
+    // or a prime)
+    while (i < nq) {
+        const uint32_t stop = nq - i > 64 ? i + 64 : nq;
+#pragma unroll 4
+        for (; i < stop; ++i) {
+            const uint4 t = tab[i];
+            const uint64_t inv = (uint64_t)t.y << 32 | t.x;
+            uint64_t x = R * inv;
+            if ((uint32_t)(x >> 32) <= t.z && __umul64hi(x, t.w) == 0) {
+                uint32_t v = 0;
+                do {  // x = R / q
+                    R = x;
+                    S *= t.w;
+                    ++v;
+                    x = R * inv;
+                } while (__umul64hi(x, t.w) == 0);
+                if (nf < 16) {
+                    fq[nf] = t.w;
+                    fv[nf] = v;
+                }
+                ++nf;
+            }
+        }
+        if (i < nq) {
+            const uint64_t q = tab[i].w;
+            if (q * q > R)
+                break;
+        }
+    }
+    if (R > 1 && R <= bmax) {
+        // stopped early with a prime cofactor no larger than bmax (after a
+        // full pass R keeps only prime factors above bmax)
+        if (nf < 16) {
+            fq[nf] = (uint32_t)R;
+            fv[nf] = 1;
+        }
+        ++nf;
+        S *= R;
+        R = 1;
+    }
+    Mont m;
+    m.init(p);
+    uint64_t f0, f1;
+    fib_pair(m, S, f0, f1);
+    if (f0 != 0)
+        return;  // a(p) does not divide S: no hits below e
+    // a(p): S with each prime taken out while F stays zero, the largest
+    // primes first (D < 2^63 has at most 15 odd prime factors, so fq holds
+    // them all).  Once a prime is done, its power in a(p) is final; when the
+    // product of the final parts exceeds what the hits allow, stop.
+    const uint64_t amax = FAM == FIBONACCI ? bmax : 2 * bmax;
+    uint64_t a = S, fixed = 1;
+    for (int k = (nf < 16 ? nf : 16) - 1; k >= -1; --k) {
+        const uint64_t q = k >= 0 ? fq[k] : 2;
+        const uint32_t v = k >= 0 ? fv[k] : (uint32_t)v2;
+        uint32_t t = 0;
+        for (; t < v; ++t) {
+            fib_pair(m, a / q, f0, f1);
+            if (f0 != 0)
+                break;
+            a /= q;
+        }
+        for (uint32_t r = t; r < v && fixed <= amax; ++r)
+            fixed *= q;
+        if (fixed > amax)
+            return;
+    }
+    uint64_t first, step = a;
+    if (FAM == FIBONACCI) {
+        first = (s + a - 1) / a * a;
+    } else {
+        if (a & 1)
+            return;
+        const uint64_t h = a >> 1;  // n = h mod a
+        const uint64_t r = s % a;
+        first = s + (h >= r ? h - r : a - r + h);
+    }
+    for (uint64_t n = first; n < e; n += step)
+        push(job.fb, n - job.n0, p);
+}
+
 // Fibonacci / Lucas: state (S(n-1), S(n)), one addmod per step
 // (fibonacci.hpp:245-285, lucas.hpp:394-418).  The reference's
 // make_state(0) leaves S(-1) = 0 and S(0) = 0, so a job starting at n0 = 0
@@ -586,6 +770,15 @@ __device__ __forceinline__ void fib_pair(const Mont &m, uint64_t k, uint64_t &fk
 template <uint32_t FAM>
 __device__ __forceinline__ void run_fibonacci(const JobView &job, uint64_t p, uint64_t s, uint64_t e)
 {
+    // the rank-of-apparition path costs about 8 operations per table prime
+    // up to e plus ~2000 for its Fibonacci evaluations, the walk about 5 per
+    // term: taken when 5 (e - s) > 8 pi(e) + 2000, with pi(e) < 1.26 e / ln e
+    // <= e / 5 (e >= 2^10) and exact enough for this choice
+    if (job.n0 != 0 && s != 0 && (p & 1) && p != 5 && p < (1ull << 62) && e <= TRIAL_LIMIT &&
+        (e - s) * 6 > e + 2400 && job.variant != CTD_VARIANT_WALK) {
+        run_fibonacci_rank<FAM>(job, p, s, e);
+        return;
+    }
     uint64_t a = 0, b = 0;  // (S(s-1), S(s))
     if (job.n0 != 0 && s != 0) {
         Mont m;
@@ -1404,6 +1597,44 @@ __global__ void mod2_kernel(JobView job)
         if (!r)
             push(job.fb, n + 1 - job.n0, 2);
     }
+}
+
+// ----------------------------------------------------- per-device tables
+int prepare_residue_tables(int device, std::string &err)
+{
+    static std::mutex mu;
+    static std::vector<int> done;
+    static std::vector<uint4> div;
+    std::lock_guard<std::mutex> lock(mu);
+    for (int d : done)
+        if (d == device)
+            return CTD_OK;
+    if (div.empty()) {
+        std::vector<uint8_t> composite(TRIAL_LIMIT, 0);
+        for (uint32_t q = 3; q < TRIAL_LIMIT; q += 2) {
+            if (composite[q])
+                continue;
+            for (uint64_t k = (uint64_t)q * q; k < TRIAL_LIMIT; k += 2ull * q)
+                composite[k] = 1;
+            uint64_t inv = q;  // q^-1 mod 2^64 by Newton steps (3, 6, ..., 96 bits)
+            for (int it = 0; it < 5; ++it)
+                inv *= 2 - (uint64_t)q * inv;
+            const uint64_t lim = ~0ull / q;
+            div.push_back(uint4{(uint32_t)inv, (uint32_t)(inv >> 32), (uint32_t)(lim >> 32), q});
+        }
+        if (div.size() != TRIAL_PRIMES) {
+            err = "trial-division table: unexpected prime count";
+            div.clear();
+            return CTD_ERR_CUDA;
+        }
+    }
+    cudaError_t rc = cudaMemcpyToSymbol(g_trial_div, div.data(), div.size() * sizeof(uint4));
+    if (rc != cudaSuccess) {
+        err = std::string("trial-division table upload: ") + cudaGetErrorString(rc);
+        return CTD_ERR_CUDA;
+    }
+    done.push_back(device);
+    return CTD_OK;
 }
 
 // ----------------------------------------------------------- launchers

@@ -151,9 +151,13 @@ int ctd_check_job(const ctd_job *job);
  *
  * counts_inout[n1-n0] and factors_inout[(n1-n0)*max_factors] use the
  * reference factors_buffer layout (src/factors_buffer.hpp:77-86); on entry
- * they hold the resume state (zeros for a fresh job), on return the result
- * (slot order is arrival order: sort per term before printing, as
- * src/factors_buffer.hpp:123-138 does).  Primes p <= resume_after_prime are
+ * they hold the resume state (zeros for a fresh job; slots past a term's
+ * count must be zero), on return the result (slot order is arrival order:
+ * sort per term before printing, as src/factors_buffer.hpp:123-138 does).
+ * A term with more prime factors in range than max_factors keeps the
+ * max_factors smallest and its count exceeds max_factors: the CPU engine's
+ * result; the reference's device push keeps whichever arrive first and both
+ * report the excess (src/factors_buffer.hpp:62-75).  Primes p <= resume_after_prime are
  * skipped (src/trial_factoring.cuh:404).  segment_length 0 = default 2^26.
  */
 int ctd_run_plain(ctd_ctx *ctx, const ctd_job *job, uint32_t *counts_inout, uint64_t *factors_inout,
@@ -175,7 +179,8 @@ int ctd_sieve_device(ctd_ctx *ctx, uint64_t lo, uint64_t hi, uint64_t *d_out, ui
                      uint64_t *count, void *stream);
 
 /* The residue kernel over an explicit list of odd primes in device memory,
- * pushing hits into a device factors buffer.  The unit that
+ * pushing hits into a device factors buffer (slots past a term's count
+ * zero, as for ctd_run_plain).  The unit that
  * trial_div_by_odd_primes<Seq, 1, ...> implements (src/trial_factoring.cuh:156-228).
  * Asynchronous on `stream`. */
 int ctd_residues_device(ctd_ctx *ctx, const ctd_job *job, const uint64_t *d_primes, uint64_t nprimes,
