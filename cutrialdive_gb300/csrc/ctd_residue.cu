@@ -54,6 +54,8 @@ __device__ __forceinline__ void push_overflow(unsigned long long *slots, uint32_
         unsigned long long m = 0, raw = 0;
         uint32_t j = 0;
         if (lane == leader) {
+            // volatile loads: another SM's exchanges must show (the
+            // exchange below checks what they read); an empty slot ends it
             for (uint32_t i = 0; i < k; ++i) {
                 const unsigned long long v = *(volatile unsigned long long *)&slots[i];
                 const unsigned long long key = v ? v : ~0ull;
@@ -106,6 +108,12 @@ __device__ __forceinline__ void push(const FactorsView &fb, uint64_t idx, uint64
     if (__builtin_expect(__any_sync(peers, pending), 0))
         push_overflow(slots, fb.max_factors, p, pending, peers, leader);
 }
+
+// push out of line, for the baby-step families (doubling, fixed-n): one call
+// per site keeps their short walks compact (with the push inlined at every
+// site, walks of a few blocks ran 24 % slower), while an out-of-line push in
+// the Smarandache walk's loop cost it 2.5x, so the others keep push inlined
+__device__ __noinline__ void push_call(const FactorsView &fb, uint64_t idx, uint64_t p) { push(fb, idx, p); }
 
 // ------------------------------------------------------- step primitives
 // For p < 2^63 the modular double / add is: v = a + b - p (one 3-input add
@@ -180,7 +188,7 @@ __device__ __forceinline__ void walk_target(uint64_t u, uint64_t target, uint64_
                                             const FactorsView &fb, Step step)
 {
     if (u == target)
-        push(fb, idx, p);
+        push_call(fb, idx, p);
     const uint32_t tlo = (uint32_t)target;
     uint64_t i = 0;
     for (; i + UNROLL <= steps; i += UNROLL) {
@@ -197,14 +205,14 @@ __device__ __forceinline__ void walk_target(uint64_t u, uint64_t target, uint64_
             for (int j = 0; j < UNROLL; ++j) {
                 v = step(v);
                 if (v == target)
-                    push(fb, idx + i + j + 1, p);
+                    push_call(fb, idx + i + j + 1, p);
             }
         }
     }
     for (; i < steps; ++i) {
         u = step(u);
         if (u == target)
-            push(fb, idx + i + 1, p);
+            push_call(fb, idx + i + 1, p);
     }
 }
 
@@ -216,7 +224,7 @@ __device__ __forceinline__ void walk_add63(uint64_t u, uint64_t c, uint64_t targ
                                            uint64_t steps, const FactorsView &fb)
 {
     if (u == target)
-        push(fb, idx, p);
+        push_call(fb, idx, p);
     const uint32_t tlo = (uint32_t)target;
     uint64_t nb = steps / UNROLL;
     uint64_t base = idx;  // index of the state before the current block
@@ -231,7 +239,7 @@ __device__ __forceinline__ void walk_add63(uint64_t u, uint64_t c, uint64_t targ
                 for (int j = 0; j < UNROLL; ++j) {
                     v = DOUBLE ? add63(v, v, p) : add63(v, c, p);
                     if (v == target)
-                        push(fb, at + j + 1, p);
+                        push_call(fb, at + j + 1, p);
                 }
             }
         }
@@ -241,7 +249,7 @@ __device__ __forceinline__ void walk_add63(uint64_t u, uint64_t c, uint64_t targ
     for (uint64_t i = base - idx; i < steps; ++i) {
         u = DOUBLE ? add63(u, u, p) : add63(u, c, p);
         if (u == target)
-            push(fb, idx + i + 1, p);
+            push_call(fb, idx + i + 1, p);
     }
 }
 
@@ -550,14 +558,14 @@ __device__ __forceinline__ void run_doubling(const JobView &job, uint64_t p, uin
 #pragma unroll 1
             for (int j = 0; j < BS; ++j) {
                 if (v == wt)
-                    push(job.fb, at0 + b * BS + j, p);
+                    push_call(job.fb, at0 + b * BS + j, p);
                 v = half63(v, p);
             }
         };
         w = run_blocks(tlo, w, nb, giant, replay);
         for (uint64_t n = s + nb * BS; n < e; ++n) {  // the short tail, term by term
             if (w == wt)
-                push(job.fb, n - job.n0, p);
+                push_call(job.fb, n - job.n0, p);
             w = half63(w, p);
         }
     } else if (p < (1ull << 63))
@@ -598,7 +606,7 @@ __device__ __forceinline__ void run_fixed_n(const JobView &job, uint64_t p, uint
 #pragma unroll 1
             for (int j = 0; j < BS; ++j) {
                 if (x == target)
-                    push(job.fb, at0 + b * BS + j, p);
+                    push_call(job.fb, at0 + b * BS + j, p);
                 x = add63(x, c, p);
             }
         };
