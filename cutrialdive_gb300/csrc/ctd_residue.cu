@@ -778,12 +778,12 @@ __device__ void run_fibonacci_rank(const JobView &job, uint64_t p, uint64_t s, u
 template <uint32_t FAM>
 __device__ __forceinline__ void run_fibonacci(const JobView &job, uint64_t p, uint64_t s, uint64_t e)
 {
-    // the rank-of-apparition path costs about 8 operations per table prime
-    // up to e plus ~2000 for its Fibonacci evaluations, the walk about 5 per
-    // term: taken when 5 (e - s) > 8 pi(e) + 2000, with pi(e) < 1.26 e / ln e
-    // <= e / 5 (e >= 2^10) and exact enough for this choice
+    // measured on a GB300, a table prime of the rank-of-apparition path costs
+    // about 3.9 terms of the walk: taken when e - s > 3.9 pi(e), with pi(e) ~
+    // e / ln e and ln e ~ 0.69 floor(log2 e), i.e. (e - s) floor(log2 e) >
+    // 6 e (+4096 for its fixed cost)
     if (job.n0 != 0 && s != 0 && (p & 1) && p != 5 && p < (1ull << 62) && e <= TRIAL_LIMIT &&
-        (e - s) * 6 > e + 2400 && job.variant != CTD_VARIANT_WALK) {
+        (e - s) * (uint64_t)(63 - __clzll(e)) > 6 * e + 4096 && job.variant != CTD_VARIANT_WALK) {
         run_fibonacci_rank<FAM>(job, p, s, e);
         return;
     }
