@@ -82,7 +82,7 @@ FAMILY_NAMES = {0: "MERSENNE", 1: "PROTH", 2: "RIESEL", 3: "SMARANDACHE", 4: "FI
 #  * doubling (Proth/Riesel/Mersenne): baby-step/giant-step blocks of 32
 #    terms through a per-prime target filter: per block a slot shift, a field
 #    shift, two funnel-shift bit tests, their AND and the OR into the vote of
-#    a group of four blocks (6), the 32 exact compares on the ~5.5% of
+#    a group of eight blocks (6), the 32 exact compares on the ~5.5% of
 #    warp-blocks some lane passes (~2); the giant step (a 32-bit Montgomery
 #    reduction) and the hash multiply are on the multiply pipe -> 8/32;
 #  * fixed-n: the same filtered blocks, giant step a modular add (5) -> 13/32;

@@ -441,7 +441,7 @@ __device__ __forceinline__ uint64_t plain_blocks(const uint32_t (&tlo)[BS], uint
 // never splits).  That path keeps only the group's first state and steps
 // from it, so little stays live across the loop (the targets fill 32
 // registers) and its code exists once.
-constexpr int FILTER_GROUP = 4;
+constexpr int FILTER_GROUP = 8;
 template <typename Step, typename Replay>
 __device__ __forceinline__ uint64_t filtered_groups(const uint32_t (&tlo)[BS], uint64_t x, uint64_t ng, Step step,
                                                     Replay replay)
@@ -692,7 +692,7 @@ __device__ void run_fibonacci_rank(const JobView &job, uint64_t p, uint64_t s, u
     // or a prime)
     while (i < nq) {
         const uint32_t stop = nq - i > 64 ? i + 64 : nq;
-#pragma unroll 4
+#pragma unroll 8
         for (; i < stop; ++i) {
             const uint4 t = tab[i];
             const uint64_t inv = (uint64_t)t.y << 32 | t.x;
