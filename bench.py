@@ -97,10 +97,11 @@ FAMILY_NAMES = {0: "MERSENNE", 1: "PROTH", 2: "RIESEL", 3: "SMARANDACHE", 4: "FI
 ALU_OPS_PER_UPDATE = {0: 8 / 32, 1: 8 / 32, 2: 8 / 32, 6: 13 / 32, 7: 13 / 32, 4: 50 / 16, 5: 50 / 16, 8: 39 / 12,
                       3: 6}
 # DRAM bytes per prime of residue_kernel<PROTH> from one ncu capture on
-# [2^32, 2^32 + 2^27): 48,436,480 + 1,024 bytes for 6,047,768 primes; each
-# prime is read once per launch, so a full launch's traffic is this figure
-# times its primes
-DRAM_BYTES_PER_PRIME = (48436480 + 1024) / 6047768
+# [2^32, 2^32 + 2^27): 48,680,960 read + 3,608,320 written for 6,047,768
+# primes (each prime read once per launch; the writes are the factors buffer,
+# cleared at the start of the step, going back from L2), so a full launch's
+# traffic is this figure times its primes
+DRAM_BYTES_PER_PRIME = (48680960 + 3608320) / 6047768
 
 
 def mv_bound(y: int) -> int:
