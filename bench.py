@@ -90,11 +90,11 @@ FAMILY_NAMES = {0: "MERSENNE", 1: "PROTH", 2: "RIESEL", 3: "SMARANDACHE", 4: "FI
 #    add (2) and the zero-test compare (1) per step, plus one shift per state
 #    for the block-end reduction (2 per 16 steps) -> 3.125; the test's
 #    multiply and the reduction's multiply-adds run on the multiply pipe;
-#  * tribonacci (p < 2^40): blocks of 12 steps: a three-input 64-bit add (2)
-#    and the compare (1) per step, 3 shifts per block -> 3.25;
+#  * tribonacci (p < 2^40): blocks of 18 steps: a three-input 64-bit add (2)
+#    and the compare (1) per step, 3 shifts per block -> 57/18;
 #  * Smarandache (64-bit Shoup): adds/subtracts of x M + m - q p (4) and
 #    two low-word compares = 6, plus 9 32-bit multiplies.
-ALU_OPS_PER_UPDATE = {0: 8 / 32, 1: 8 / 32, 2: 8 / 32, 6: 13 / 32, 7: 13 / 32, 4: 50 / 16, 5: 50 / 16, 8: 39 / 12,
+ALU_OPS_PER_UPDATE = {0: 8 / 32, 1: 8 / 32, 2: 8 / 32, 6: 13 / 32, 7: 13 / 32, 4: 50 / 16, 5: 50 / 16, 8: 57 / 18,
                       3: 6}
 # DRAM bytes per prime of residue_kernel<PROTH> from one ncu capture on
 # [2^32, 2^32 + 2^27): 48,680,960 read + 3,608,320 written for 6,047,768

@@ -1004,9 +1004,13 @@ __device__ __forceinline__ void run_tribonacci(const JobView &job, uint64_t p, u
     if (p < (1ull << 40)) {
         Lazy lz;
         lz.init(m);
-        constexpr int TB = 12;  // steps per block
+        constexpr int TB = 18;  // steps per block (a multiple of 3: the roles rotate back)
         // bounds K[j] (in the PTX below): values after step j of a block are
-        // below K[j] p = 9, 15, 27, 51, ... 6627 p (from states below 3p)
+        // below K[j] p = 9, 15, 27, 51, ... 256575 p (from states below 3p;
+        // K[j] = K[j-1] + K[j-2] + K[j-3]), so below 2^58 for p < 2^40 and
+        // within Lazy::reduce's range (K < 2^31); a non-multiple passes the
+        // test of step j with probability K[j] / 2^32, so a lane-block sees a
+        // false candidate about once in 7600
         uint64_t nb = steps / TB;
         while (nb) {
           const uint32_t chunk = nb > 0x40000000ull ? 0x40000000u : (uint32_t)nb;
@@ -1024,6 +1028,9 @@ __device__ __forceinline__ void run_tribonacci(const JobView &job, uint64_t p, u
                 CTD_LZ3_STEP("%0", "%1", "%2", 315) CTD_LZ3_STEP("%1", "%2", "%0", 579)
                 CTD_LZ3_STEP("%2", "%0", "%1", 1065) CTD_LZ3_STEP("%0", "%1", "%2", 1959)
                 CTD_LZ3_STEP("%1", "%2", "%0", 3603) CTD_LZ3_STEP("%2", "%0", "%1", 6627)
+                CTD_LZ3_STEP("%0", "%1", "%2", 12189) CTD_LZ3_STEP("%1", "%2", "%0", 22419)
+                CTD_LZ3_STEP("%2", "%0", "%1", 41235) CTD_LZ3_STEP("%0", "%1", "%2", 75843)
+                CTD_LZ3_STEP("%1", "%2", "%0", 139497) CTD_LZ3_STEP("%2", "%0", "%1", 256575)
                 "selp.u32 %3, 1, 0, c;\n\t}"
                 : "+l"(x), "+l"(y), "+l"(z), "=r"(cand)
                 : "r"(lz.pinv32));
