@@ -443,8 +443,8 @@ def run_ours(args, world, rank, local):
     }
     if fam == 1:
         roofline["traffic"] = DRAM_BYTES_PER_PRIME * statistics.mean(nodd)
-        roofline["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of a 2^27-segment launch, "
-                                      "scaled by primes per launch (profiles/residue_kernel_proth_k3_seg2p27_full.md)")
+        roofline["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one 2^27-segment launch "
+                                      "of this kernel, scaled by the primes per launch")
     else:
         roofline["traffic"] = None
     roofline["algorithmic_bytes"] = 8 * statistics.mean(nodd)

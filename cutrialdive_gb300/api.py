@@ -212,7 +212,11 @@ def write_checkpoint(path: str, spec: num_seq_spec, opts: trial_factoring_option
         b.write(struct.pack("=I", c))
         b.write(f[i, : min(c, m)].astype("=u8").tobytes())
     tmp = f"{path}.tmp_{time.time_ns()}"
-    with open(tmp, "wb") as fh:
+    try:
+        fh = open(tmp, "wb")
+    except OSError:  # the reference's message (src/checkpoint.cpp:181-184)
+        raise RuntimeError(f"Could not create temporary file `{tmp}'") from None
+    with fh:
         fh.write(b.getvalue())
     os.replace(tmp, path)
 

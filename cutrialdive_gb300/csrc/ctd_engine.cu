@@ -20,6 +20,7 @@ struct ctd_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     SieveWorkspace *ws = nullptr;
+    ResidueScratch *rs = nullptr;
     std::string last_error;
     int grid_override = 0;
     int block_override = 0;
@@ -186,6 +187,12 @@ uint32_t variant_of(const ctd_ctx *ctx, uint32_t family)
     return t ? t->variant : CTD_VARIANT_AUTO;
 }
 
+uint32_t classify_min_of(const ctd_ctx *ctx, uint32_t family)
+{
+    const ctd_tuning *t = tuning_of(ctx, family);
+    return t && t->classify_min ? t->classify_min : DEFAULT_CLASSIFY_MIN;
+}
+
 uint64_t default_segment(const ctd_ctx *ctx, uint32_t family)
 {
     const ctd_tuning *t = tuning_of(ctx, family);
@@ -267,13 +274,23 @@ int ctd_open(int device, ctd_ctx **out)
     // device tables of the residue kernels, uploaded before any launch or
     // graph capture on this device
     std::string terr;
-    const int trc = prepare_residue_tables(device, terr);
+    int trc = prepare_residue_tables(device, terr);
+    if (trc == CTD_OK)
+        trc = noalloc_prepare(device, terr);
     if (trc != CTD_OK) {
         cudaStreamDestroy(ctx->stream);
         delete ctx;
         return trc;
     }
     ctx->ws = sieve_workspace_create();
+    ctx->rs = residue_scratch_create(device, ctx->sm_count);
+    if (!ctx->ws || !ctx->rs) {
+        sieve_workspace_destroy(ctx->ws);
+        residue_scratch_destroy(ctx->rs);
+        cudaStreamDestroy(ctx->stream);
+        delete ctx;
+        return CTD_ERR_OUT_OF_MEMORY;
+    }
     *out = ctx;
     return CTD_OK;
 }
@@ -286,6 +303,7 @@ void ctd_close(ctd_ctx *ctx)
     if (ctx->stream)
         cudaStreamSynchronize(ctx->stream);
     sieve_workspace_destroy(ctx->ws);
+    residue_scratch_destroy(ctx->rs);
     cudaFree(ctx->d_primes);
     cudaFree(ctx->d_counts);
     cudaFree(ctx->d_factors);
@@ -405,12 +423,13 @@ int ctd_autotune(ctd_ctx *ctx, const ctd_job *job, double budget_s, ctd_tuning *
         const int grid = grid_for(ctx, job->family, c.block_size, c.ctas_per_sm);
         tiles_for(n, N, grid, c.block_size, c.items_per_thread, c.min_tile, view.tiles, view.tile_len);
         view.variant = c.variant;
+        view.classify_min = c.classify_min ? c.classify_min : DEFAULT_CLASSIFY_MIN;
         ms = 1e30f;
         for (int r = 0; r < 3; ++r) {
             if (cudaMemsetAsync(ctx->d_counts, 0, N * sizeof(uint32_t), st) != cudaSuccess)
                 return CTD_ERR_CUDA;
             cudaEventRecord(ea, st);
-            int e = launch_residues(view, ctx->d_primes, n, grid, c.block_size, st, err);
+            int e = launch_residues(view, ctx->d_primes, n, grid, c.block_size, st, err, ctx->rs);
             if (e)
                 return e;
             cudaEventRecord(eb, st);
@@ -567,11 +586,12 @@ int ctd_residues_device(ctd_ctx *ctx, const ctd_job *job, const uint64_t *d_prim
     cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
     JobView v = make_view(job, d_counts, d_factors);
     v.variant = variant_of(ctx, job->family);
+    v.classify_min = classify_min_of(ctx, job->family);
     const int block = default_block(ctx, job->family);
     const int grid = default_grid(ctx, job->family, block);
     choose_tiles(ctx, job->family, nprimes, job->n1 - job->n0, grid, block, v.tiles, v.tile_len);
     std::string err;
-    int rc = launch_residues(v, d_primes, nprimes, grid, block, st, err);
+    int rc = launch_residues(v, d_primes, nprimes, grid, block, st, err, ctx->rs);
     return rc ? fail(ctx, rc, err) : CTD_OK;
 }
 
@@ -612,6 +632,7 @@ int ctd_run_plain(ctd_ctx *ctx, const ctd_job *job, uint32_t *counts_inout, uint
     CTX_CUDA(cudaMemcpyAsync(ctx->d_factors, factors_inout, NF * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
     JobView view = make_view(job, ctx->d_counts, ctx->d_factors);
     view.variant = variant_of(ctx, job->family);
+    view.classify_min = classify_min_of(ctx, job->family);
     std::string err;
 
     uint64_t f0 = resume_after_prime ? resume_after_prime + 1 : job->f0;
@@ -641,7 +662,7 @@ int ctd_run_plain(ctd_ctx *ctx, const ctd_job *job, uint32_t *counts_inout, uint
             return fail(ctx, CTD_ERR_CAPACITY, "prime count above its bound");
         if (np) {
             choose_tiles(ctx, job->family, np, N, grid, block, view.tiles, view.tile_len);
-            rc = launch_residues(view, ctx->d_primes, np, grid, block, st, err);
+            rc = launch_residues(view, ctx->d_primes, np, grid, block, st, err, ctx->rs);
             if (rc)
                 return fail(ctx, rc, err);
             uint64_t lp = 0;

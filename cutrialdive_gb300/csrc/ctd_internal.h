@@ -42,6 +42,7 @@ struct JobView {
     uint32_t family;
     uint32_t tiles;      // index tiles per prime (>= 1)
     uint32_t variant;    // step form (CTD_VARIANT_*)
+    uint32_t classify_min;  // doubling families: index ranges this long or longer walk power-residue classes
     uint64_t param;      // k, n or base
     uint64_t n0, n1;     // index range of the factors buffer
     uint64_t tile_len;   // indices per tile (last tile may be shorter)
@@ -93,16 +94,38 @@ uint64_t sieve_scratch_base_windows(uint64_t limit);
 // to read the count.
 int sieve_range_scratch(const SieveScratch &sc, int sm_count, uint64_t lo, uint64_t hi, uint64_t *d_out,
                         uint64_t capacity, uint64_t *count, cudaStream_t stream, std::string &err);
+// Looks up the allocation-free sieve's static scratch on `device` (the
+// current device), which places it there; called when a context opens.
+int noalloc_prepare(int device, std::string &err);
 
 // -------------------------------------------------------------- residues
+// Scratch of the classified doubling launches (Proth, Riesel, Mersenne over
+// long index ranges): per prime its power-residue class, then the primes
+// regrouped by class so a warp's lanes walk classes of equal length.  Owned
+// by a context; grown on demand (never during a graph capture).
+struct ClassCounters;
+struct ClassItem;
+struct ResidueScratch {
+    int device = 0;
+    int sm_count = 1;
+    uint32_t *codes = nullptr;
+    ClassItem *items = nullptr;
+    uint64_t cap = 0;  // primes
+    ClassCounters *counters = nullptr;
+};
+ResidueScratch *residue_scratch_create(int device, int sm_count);
+void residue_scratch_destroy(ResidueScratch *rs);
+// default length from which the doubling families walk power-residue classes
+constexpr uint32_t DEFAULT_CLASSIFY_MIN = 8192;
 // Uploads the residue kernels' per-device tables (the trial-division primes
 // of the Fibonacci/Lucas rank-of-apparition path) to `device`, the current
 // device, once per process and device.
 int prepare_residue_tables(int device, std::string &err);
 // Odd primes only.  Launches the family's residue kernel over
-// nprimes x view.tiles work items.
+// nprimes x view.tiles work items; with `scratch`, the doubling families'
+// long ranges go through the classified launches (classify, regroup, walk).
 int launch_residues(const JobView &view, const uint64_t *d_primes, uint64_t nprimes, int grid, int block,
-                    cudaStream_t stream, std::string &err);
+                    cudaStream_t stream, std::string &err, ResidueScratch *scratch = nullptr);
 // One job of a batched launch: its view (factors buffer, index range) and
 // its prime range [f0, f1).
 struct BatchJob {

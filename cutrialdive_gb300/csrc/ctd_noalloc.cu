@@ -12,11 +12,11 @@
 //
 // Limits: hi - lo <= CTD_NOALLOC_SIEVE_MAX_RANGE (2^26) and
 // hi <= CTD_NOALLOC_SIEVE_MAX_HI (2^48, so every base prime is below 2^24).
-// The array (about 8.6 MiB) is held on every GPU that loads the library
-// until the process exits.  Every call uses the same array and it keeps the
-// previous call's contents; each call rewrites everything it reads, and
-// calls that overlap on the GPU (different streams or threads at the same
-// time) race on it.
+// The array (about 8.6 MiB) is placed on a GPU when a context opens on it
+// (ctd_open looks up its address) and stays there until the process exits.
+// Every call uses the same array and it keeps the previous call's contents;
+// each call rewrites everything it reads, and calls that overlap on the GPU
+// (different streams or threads at the same time) race on it.
 #include "ctd_internal.h"
 
 #include <mutex>
@@ -71,6 +71,18 @@ int scratch_for_device(int device, unsigned char **addr, std::string &err)
 }
 
 }  // namespace
+
+// Called by ctd_open on its device: the lookup loads this file's module,
+// and with it the array, onto the device when the context opens.  Under
+// CUDA's lazy module loading the array would otherwise arrive with the
+// first allocation-free call -- possibly after the caller has reserved all
+// of the device's memory for itself.
+int noalloc_prepare(int device, std::string &err)
+{
+    unsigned char *addr = nullptr;
+    return scratch_for_device(device, &addr, err);
+}
+
 }  // namespace ctd
 
 using namespace ctd;

@@ -15,11 +15,13 @@
 // Hits are exact: a prime is pushed for index n iff p | S(n), exactly the
 // set the reference's Barrett propagation yields.
 #include "ctd_arith.cuh"
+#include "ctd_powres.cuh"
 #include "ctd_smarandache.cuh"
 #include "ctd_internal.h"
 
 #include <atomic>
 #include <mutex>
+#include <new>
 #include <vector>
 
 namespace ctd {
@@ -345,7 +347,7 @@ extern __shared__ __align__(16) uint32_t ctd_filter_smem[];
 template <uint32_t FAM>
 constexpr bool uses_filter()
 {
-    return FAM == PROTH || FAM == RIESEL || FAM == MERSENNE || FAM == PROTH_FIXED_N || FAM == RIESEL_FIXED_N;
+    return FAM == PROTH || FAM == RIESEL || FAM == MERSENNE;
 }
 
 struct TargetFilter {
@@ -574,50 +576,170 @@ __device__ __forceinline__ void run_doubling(const JobView &job, uint64_t p, uin
         walk_target(start(), target, p, s - job.n0, steps, job.fb, [p](uint64_t x) { return dblmod(x, p); });
 }
 
-// k*2^n +- 1 with fixed n over the index k (riesel_proth_fixed_n.hpp:88-151):
-// v(k) = k*2^n mod p grows by c = 2^n mod p per index; S(k) = 0 iff
-// v == p-1 (Proth) or v == 1 (Riesel).
+// ------------------------------------- doubling over power-residue classes
+// For long index ranges the doubling families first classify each prime
+// (ctd_powres.cuh): every zero n of k*2^n-+1 (2^n-1) mod p satisfies
+// n = r (mod M) for a class M | 2^6 * 3 * 5 * 7 read off the 2-power, 3rd,
+// 5th and 7th power residues of 2 and of the target, and about 40 % of the
+// primes (Proth k = 3) divide no term at all.  The walk then visits only
+// n = r, r + M, r + 2M, ... with the same baby-step/giant-step blocks over
+// w(n) = 2^-n: block b's 32 terms are zeros iff its state equals one of the
+// targets wt * 2^(M j), the giant step multiplies by 2^-32M.  Every term of
+// the class is still tested exactly, so the hits are those of the full walk.
+
+// x * w mod p for x < 2^64, w < p < 2^63, with Shoup's quotient
+// ws = floor(w 2^64 / p): x w - mulhi(x, ws) p lies in [0, 2p).
+struct MulConst {
+    uint64_t w, ws;
+    __device__ __forceinline__ uint64_t mul(uint64_t x, uint64_t p) const
+    {
+        const uint64_t q = mulhi64(x, ws);
+        const uint64_t r = x * w - q * p;
+        return r >= p ? r - p : r;
+    }
+};
+
+// the target of w(n) = 2^-n: -k (Proth), k (Riesel), 1 (Mersenne); 0 when p | k
+template <uint32_t FAM>
+__device__ __forceinline__ uint64_t doubling_target(const JobView &job, uint64_t p)
+{
+    const uint64_t k = FAM == MERSENNE ? 1 : (job.param < p ? job.param : job.param % p);
+    return FAM == PROTH ? (k ? p - k : 0) : k;
+}
+
+// code of a prime's class: M << 16 | r, 0 when p divides no term; primes of
+// 2^63 and above keep the plain walk (M = 1)
+template <uint32_t FAM>
+__device__ __forceinline__ uint32_t doubling_class_code(const JobView &job, uint64_t p)
+{
+    if (p >= (1ull << 63))
+        return 1u << 16;
+    const uint64_t wt = doubling_target<FAM>(job, p);
+    if (!wt)
+        return 0;
+    Mont m;
+    m.init(p);
+    const PowerClass c = doubling_class(m, m.to(wt));
+    return c.M ? (c.M << 16) | c.r : 0u;
+}
+
+// The doubling walk over n = r (mod M) in [s, e), p < 2^63.
+template <uint32_t FAM>
+__device__ void run_doubling_class(const JobView &job, uint64_t p, uint32_t M, uint32_t r, uint64_t s, uint64_t e)
+{
+    const uint32_t sr = (uint32_t)(s % M);
+    const uint64_t off = r >= sr ? r - sr : M - sr + r;
+    if (off >= e - s)
+        return;
+    const uint64_t nf = s + off;               // first term of the class
+    const uint64_t cnt = (e - 1 - nf) / M + 1;  // terms nf, nf + M, ... below e
+    Mont m;
+    m.init(p);
+    const uint64_t wt = doubling_target<FAM>(job, p);
+    const uint64_t nr = nf < p - 1 ? nf : nf % (p - 1);
+    uint64_t w = m.from(m.pow2(p - 1 - nr));  // 2^-nf (Fermat)
+    const uint64_t HM = small_pow(m, m.to((p + 1) >> 1), M);  // 2^-M, Montgomery form
+    const uint64_t g = m.from(HM);
+    const MulConst step{g, m.shoup(g)};  // w -> w 2^-M: the next term of the class
+    const uint64_t at0 = nf - job.n0;
+    uint64_t i = 0;
+    if (cnt >= 2 * BS) {
+        // targets wt 2^(M j), j < 32: term j of a block is a zero iff the
+        // block's state equals target j
+        const uint64_t c = m.from(m.pow2(M));
+        const MulConst up{c, m.shoup(c)};
+        uint32_t tlo[BS];
+        uint64_t t = wt;
+#pragma unroll
+        for (int j = 0; j < BS; ++j) {
+            tlo[j] = (uint32_t)t;
+            t = up.mul(t, p);
+        }
+        auto replay = [&](uint64_t v, uint64_t b) {
+#pragma unroll 1
+            for (int j = 0; j < BS; ++j) {
+                if (v == wt)
+                    push_call(job.fb, at0 + (b * BS + j) * M, p);
+                v = step.mul(v, p);
+            }
+        };
+        const uint64_t nb = cnt / BS;
+        if (M <= 2) {
+            // giant step w 2^-32M: one or two 32-bit Montgomery reductions
+            const uint32_t plo = (uint32_t)p, phi = (uint32_t)(p >> 32), pinv32 = (uint32_t)m.pinv;
+            const uint32_t one = (uint32_t)(p & 1);
+            if (M == 1)
+                w = run_blocks(tlo, w, nb, [&](uint64_t x) { return redc32(x, plo, phi, pinv32, one); }, replay);
+            else
+                w = run_blocks(tlo, w, nb,
+                               [&](uint64_t x) { return redc32(redc32(x, plo, phi, pinv32, one), plo, phi, pinv32, one); },
+                               replay);
+        } else {
+            const uint64_t G = m.from(square_n(m, HM, 5));  // 2^-32M
+            const MulConst giant{G, m.shoup(G)};
+            w = run_blocks(tlo, w, nb, [&](uint64_t x) { return giant.mul(x, p); }, replay);
+        }
+        i = nb * BS;
+    }
+    for (; i < cnt; ++i) {  // the tail, term by term
+        if (w == wt)
+            push_call(job.fb, at0 + i * M, p);
+        w = step.mul(w, p);
+    }
+}
+
+// warp-aggregated atomicAdd of 1 per lane on counter[key] (lanes with the
+// same key share one atomic); returns this lane's old value
+__device__ __forceinline__ uint32_t aggregated_increment(uint32_t *counter, uint32_t key)
+{
+    const uint32_t act = __activemask();
+    const uint32_t peers = __match_any_sync(act, key);
+    const int leader = __ffs(peers) - 1;
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t base = 0;
+    if ((int)lane == leader)
+        base = atomicAdd(&counter[key], (uint32_t)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    return base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+}
+
+// k*2^n +- 1 with fixed n over the index k (riesel_proth_fixed_n.hpp:88-151).
+// The reference walks v(k) = k*2^n mod p term by term (S(k) = 0 iff v ==
+// p-1 for Proth, v == 1 for Riesel).  The congruence is linear in k: p
+// divides S(k) iff k = -+2^-n (mod p), so the zeros in [s, e) are k0, k0 + p,
+// k0 + 2p, ... from the first k0 >= s of that class -- one power of 2 per
+// prime and no walk; the pushed (k, p) pairs are exactly the walk's.
+// CTD_VARIANT_WALK keeps the term-by-term walk (a second algorithm for the
+// cross-checks).
 template <uint32_t FAM>
 __device__ __forceinline__ void run_fixed_n(const JobView &job, uint64_t p, uint64_t s, uint64_t e)
 {
     Mont m;
     m.init_lite(p);
-    const uint64_t C = m.pow2(job.param);  // 2^n in Montgomery form
-    const uint64_t c = m.from(C);
-    const uint64_t v = m.mul(C, s < p ? s : s % p);  // plain s*2^n mod p
-    const uint64_t target = (FAM == PROTH_FIXED_N) ? p - 1 : 1;
-    const uint64_t steps = e - s - 1;
-    const uint64_t nblk = (e - s) / BS;
-    if (p < (1ull << 63) && nblk >= 2 && job.variant != CTD_VARIANT_WALK) {
-        uint32_t tlo[BS];
-        uint64_t t = target, W = c;
-        const uint64_t nc = p - c == p ? 0 : p - c;  // -c mod p
-#pragma unroll
-        for (int j = 0; j < BS; ++j) {
-            tlo[j] = (uint32_t)t;
-            t = addmod(t, nc, p);
-        }
-#pragma unroll
-        for (int j = 0; j < 5; ++j)  // BS c = 2^5 c
-            W = dblmod(W, p);
-        const uint64_t at0 = s - job.n0;  // index of the first term
-        auto giant = [&](uint64_t x) { return add63(x, W, p); };
-        auto replay = [&](uint64_t x, uint64_t b) {
-#pragma unroll 1
-            for (int j = 0; j < BS; ++j) {
-                if (x == target)
-                    push_call(job.fb, at0 + b * BS + j, p);
-                x = add63(x, c, p);
-            }
-        };
-        const uint64_t vb = run_blocks(tlo, v, nblk, giant, replay);
-        const uint64_t ts = s + nblk * BS;
-        if (ts < e)
-            walk_add63<false>(vb, c, target, p, ts - job.n0, e - ts - 1, job.fb);
-    } else if (p < (1ull << 63))
-        walk_add63<false>(v, c, target, p, s - job.n0, steps, job.fb);
-    else
-        walk_target(v, target, p, s - job.n0, steps, job.fb, [p, c](uint64_t x) { return addmod(x, c, p); });
+    if (job.variant == CTD_VARIANT_WALK) {
+        const uint64_t C = m.pow2(job.param);  // 2^n in Montgomery form
+        const uint64_t c = m.from(C);
+        const uint64_t v = m.mul(C, s < p ? s : s % p);  // plain s*2^n mod p
+        const uint64_t target = (FAM == PROTH_FIXED_N) ? p - 1 : 1;
+        if (p < (1ull << 63))
+            walk_add63<false>(v, c, target, p, s - job.n0, e - s - 1, job.fb);
+        else
+            walk_target(v, target, p, s - job.n0, e - s - 1, job.fb, [p, c](uint64_t x) { return addmod(x, c, p); });
+        return;
+    }
+    // u = 2^-n = 2^(p-1-(n mod (p-1))) (Fermat; p odd, so 2 is invertible)
+    const uint64_t nr = job.param < p - 1 ? job.param : job.param % (p - 1);
+    const uint64_t u = m.from(m.pow2(p - 1 - nr));
+    const uint64_t k0 = FAM == PROTH_FIXED_N ? p - u : u;  // u in [1, p-1]
+    const uint64_t sr = s < p ? s : s % p;
+    const uint64_t off = k0 >= sr ? k0 - sr : p - sr + k0;  // first k >= s with k = k0 (mod p)
+    if (off >= e - s)
+        return;
+    for (uint64_t k = s + off;; k += p) {
+        push(job.fb, k - job.n0, p);
+        if (e - k <= p)
+            break;
+    }
 }
 
 // (F(k), F(k+1)) mod p in Montgomery form by the doubling identities
@@ -1338,14 +1460,13 @@ __device__ __forceinline__ void run_peano(const JobView &job, uint64_t p, uint64
     }
 }
 
-// Resident CTAs of 256 threads the register budget is sized for (64
-// registers a thread): the baby-step families keep 32 targets in registers,
-// the others carry block-start copies and reduction constants.
+// Resident CTAs of 256 threads the register budget is sized for: the
+// baby-step families keep 32 targets in registers, the linear recurrences
+// and Smarandache carry block-start copies and reduction constants, the
+// fixed-n solve and Peano hold a few values.
 constexpr int min_ctas_per_sm(uint32_t fam)
 {
-    return fam == PEANO ? 6
-                        : (fam == PROTH || fam == RIESEL || fam == MERSENNE || fam == PROTH_FIXED_N || fam == RIESEL_FIXED_N) ? 3
-                                                                                                                   : 4;
+    return fam == PEANO ? 6 : (fam == PROTH || fam == RIESEL || fam == MERSENNE) ? 3 : 4;
 }
 
 template <uint32_t FAM>
@@ -1384,6 +1505,120 @@ residue_kernel(JobView job, const uint64_t *__restrict__ primes, uint64_t nprime
         uint64_t e = s + job.tile_len < job.n1 ? s + job.tile_len : job.n1;
         if (s < e)
             run_item<FAM>(job, primes[i], s, e);
+    }
+}
+
+// ------------------------------------------ classified doubling launches
+// classify -> regroup -> walk, all on the stream, no host wait:
+//   classify_kernel: each prime's class code and a count per class;
+//   regroup_kernel:  the primes (with their codes) written class by class,
+//                    smallest M (the longest walks) first;
+//   class_walk_kernel: a persistent grid whose warps take 32 consecutive
+//                    (prime, tile) items from a counter, so a warp's lanes
+//                    walk classes of the same M -- equal lengths, no lane
+//                    waiting on a longer one.
+// The classes are the divisors of 2^6 * 105 (56 of them), ranked by size.
+constexpr uint32_t CLASS_BUCKETS = 56;
+
+struct ClassCounters {
+    uint32_t count[CLASS_BUCKETS];  // primes per class
+    uint32_t fill[CLASS_BUCKETS];   // regroup cursors
+    unsigned long long next;        // walk work counter
+};
+
+struct ClassItem {
+    uint64_t p;
+    uint32_t code;
+    uint32_t pad;
+};
+
+// rank of M among the divisors of 2^6 * 3 * 5 * 7
+__device__ __forceinline__ uint32_t class_bucket(uint32_t M)
+{
+    uint32_t rank = 0;
+#pragma unroll
+    for (int i = 0; i <= POWRES_MAX_2EXP; ++i)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const uint32_t d = (1u << i) * ((q & 1) ? 3u : 1u) * ((q & 2) ? 5u : 1u) * ((q & 4) ? 7u : 1u);
+            rank += d < M;
+        }
+    return rank;
+}
+
+template <uint32_t FAM>
+__global__ void __launch_bounds__(256) classify_kernel(JobView job, const uint64_t *__restrict__ primes,
+                                                       uint64_t nprimes, uint32_t *__restrict__ codes,
+                                                       ClassCounters *__restrict__ cc)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nprimes; i += stride) {
+        const uint32_t code = doubling_class_code<FAM>(job, primes[i]);
+        codes[i] = code;
+        if (code)
+            aggregated_increment(cc->count, class_bucket(code >> 16));
+    }
+}
+
+__global__ void __launch_bounds__(256) regroup_kernel(const uint64_t *__restrict__ primes, uint64_t nprimes,
+                                                      const uint32_t *__restrict__ codes, ClassCounters *__restrict__ cc,
+                                                      ClassItem *__restrict__ items)
+{
+    __shared__ uint32_t base[CLASS_BUCKETS];
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (uint32_t b = 0; b < CLASS_BUCKETS; ++b) {
+            base[b] = run;
+            run += cc->count[b];
+        }
+    }
+    __syncthreads();
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nprimes; i += stride) {
+        const uint32_t code = codes[i];
+        if (code) {
+            const uint32_t b = class_bucket(code >> 16);
+            const uint32_t pos = base[b] + aggregated_increment(cc->fill, b);
+            items[pos] = ClassItem{primes[i], code, 0};
+        }
+    }
+}
+
+template <uint32_t FAM>
+__global__ void __launch_bounds__(256, min_ctas_per_sm(FAM))
+class_walk_kernel(JobView job, const ClassItem *__restrict__ items, ClassCounters *__restrict__ cc)
+{
+    __shared__ unsigned long long total_s;
+    if (threadIdx.x == 0) {
+        unsigned long long t = 0;
+        for (uint32_t b = 0; b < CLASS_BUCKETS; ++b)
+            t += cc->count[b];
+        total_s = t * job.tiles;
+    }
+    __syncthreads();
+    const unsigned long long total = total_s;
+    const uint32_t lane = threadIdx.x & 31u;
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0)
+            base = atomicAdd(&cc->next, 32ull);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= total)
+            break;
+        const uint64_t k = base + lane;
+        if (k < total) {
+            const uint64_t i = job.tiles == 1 ? k : k / job.tiles;
+            const uint64_t t = k - i * job.tiles;
+            const uint64_t s = job.n0 + t * job.tile_len;
+            const uint64_t e = s + job.tile_len < job.n1 ? s + job.tile_len : job.n1;
+            const ClassItem it = items[i];
+            if (s < e) {
+                if (it.p >= (1ull << 63))
+                    run_doubling<FAM>(job, it.p, s, e);
+                else
+                    run_doubling_class<FAM>(job, it.p, it.code >> 16, it.code & 0xffffu, s, e);
+            }
+        }
     }
 }
 
@@ -1665,11 +1900,115 @@ static cudaError_t launch_fam(const JobView &v, const uint64_t *d_primes, uint64
     return cudaGetLastError();
 }
 
+ResidueScratch *residue_scratch_create(int device, int sm_count)
+{
+    auto *rs = new (std::nothrow) ResidueScratch();
+    if (rs) {
+        rs->device = device;
+        rs->sm_count = sm_count > 0 ? sm_count : 1;
+    }
+    return rs;
+}
+
+void residue_scratch_destroy(ResidueScratch *rs)
+{
+    if (!rs)
+        return;
+    cudaFree(rs->codes);
+    cudaFree(rs->items);
+    cudaFree(rs->counters);
+    delete rs;
+}
+
+static int ensure_class_scratch(ResidueScratch *rs, uint64_t nprimes, std::string &err)
+{
+    if (!rs->counters) {
+        cudaError_t e = cudaMalloc(&rs->counters, sizeof(ClassCounters));
+        if (e != cudaSuccess) {
+            err = std::string("class counters: ") + cudaGetErrorString(e);
+            return e == cudaErrorMemoryAllocation ? CTD_ERR_OUT_OF_MEMORY : CTD_ERR_CUDA;
+        }
+    }
+    if (nprimes <= rs->cap)
+        return CTD_OK;
+    cudaFree(rs->codes);
+    cudaFree(rs->items);
+    rs->codes = nullptr;
+    rs->items = nullptr;
+    rs->cap = 0;
+    cudaError_t e = cudaMalloc(&rs->codes, nprimes * sizeof(uint32_t));
+    if (e == cudaSuccess)
+        e = cudaMalloc(&rs->items, nprimes * sizeof(ClassItem));
+    if (e != cudaSuccess) {
+        err = std::string("class scratch: ") + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? CTD_ERR_OUT_OF_MEMORY : CTD_ERR_CUDA;
+    }
+    rs->cap = nprimes;
+    return CTD_OK;
+}
+
+template <uint32_t FAM>
+static int class_walk_occupancy(int block)
+{
+    int n = 0;
+    const size_t sm = smem_bytes<FAM>(block);
+    if (allow_smem(class_walk_kernel<FAM>, sm) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, class_walk_kernel<FAM>, block, sm) != cudaSuccess)
+        return 0;
+    return n;
+}
+
+template <uint32_t FAM>
+static int launch_classified(const JobView &v, const uint64_t *d_primes, uint64_t n, cudaStream_t st,
+                             ResidueScratch *rs, std::string &err)
+{
+    int rc = ensure_class_scratch(rs, n, err);
+    if (rc)
+        return rc;
+    cudaError_t e = cudaMemsetAsync(rs->counters, 0, sizeof(ClassCounters), st);
+    const uint64_t want = (n + 255) / 256;
+    const int cgrid = (int)(want < (uint64_t)rs->sm_count * 8 ? want : (uint64_t)rs->sm_count * 8);
+    if (e == cudaSuccess) {
+        classify_kernel<FAM><<<cgrid, 256, 0, st>>>(v, d_primes, n, rs->codes, rs->counters);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        note_kernel_launch();
+        regroup_kernel<<<cgrid, 256, 0, st>>>(d_primes, n, rs->codes, rs->counters, rs->items);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        note_kernel_launch();
+        const size_t sm = smem_bytes<FAM>(256);
+        e = allow_smem(class_walk_kernel<FAM>, sm);
+        const int occ = class_walk_occupancy<FAM>(256);
+        if (e == cudaSuccess) {
+            class_walk_kernel<FAM><<<rs->sm_count * (occ > 0 ? occ : 1), 256, sm, st>>>(v, rs->items, rs->counters);
+            e = cudaGetLastError();
+        }
+    }
+    if (e != cudaSuccess) {
+        err = std::string("classified doubling launch: ") + cudaGetErrorString(e);
+        return CTD_ERR_CUDA;
+    }
+    note_kernel_launch();
+    return CTD_OK;
+}
+
 int launch_residues(const JobView &view, const uint64_t *d_primes, uint64_t nprimes, int grid, int block,
-                    cudaStream_t stream, std::string &err)
+                    cudaStream_t stream, std::string &err, ResidueScratch *scratch)
 {
     if (!nprimes || view.n1 <= view.n0)
         return CTD_OK;
+    const bool doubling = view.family == PROTH || view.family == RIESEL || view.family == MERSENNE;
+    const uint32_t cmin = view.classify_min ? view.classify_min : DEFAULT_CLASSIFY_MIN;
+    if (scratch && doubling && view.variant == CTD_VARIANT_AUTO && view.n1 - view.n0 >= cmin) {
+        switch (view.family) {
+        case PROTH: return launch_classified<PROTH>(view, d_primes, nprimes, stream, scratch, err);
+        case RIESEL: return launch_classified<RIESEL>(view, d_primes, nprimes, stream, scratch, err);
+        default: return launch_classified<MERSENNE>(view, d_primes, nprimes, stream, scratch, err);
+        }
+    }
     cudaError_t rc;
     switch (view.family) {
     case MERSENNE: rc = launch_fam<MERSENNE>(view, d_primes, nprimes, grid, block, stream); break;

@@ -349,11 +349,10 @@ static int sieve_odd(SieveWorkspace *ws, uint64_t lo_odd, uint64_t nodd, const u
     if (rc)
         return rc;
     const size_t smem = WIN_WORDS * sizeof(uint32_t);
-    static bool attr_set = false;
-    if (!attr_set) {
-        CUDA_TRY(cudaFuncSetAttribute(sieve_windows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr_set = true;
-    }
+    // a function attribute belongs to the current device: set it on every
+    // call (a host-side call, no stream work), so a context on any device
+    // launches with it
+    CUDA_TRY(cudaFuncSetAttribute(sieve_windows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int grid = grid_for(ws, nwin);
     sieve_windows<<<grid, SIEVE_THREADS, smem, st>>>(lo_odd, nodd, (uint32_t)nwin, d_base, nbase, ws->d_bits,
                                                     ws->d_wcount);

@@ -113,14 +113,18 @@ typedef struct ctd_tuning {
     uint32_t min_tile;         /* shortest index tile (each tile starts with an O(log n) jump) */
     uint32_t segment_log2;     /* default prime-segment width of ctd_run_plain, log2; 0 = 26 */
     uint32_t variant;          /* step form, CTD_VARIANT_* (results never depend on it) */
-    uint32_t reserved[2];
+    uint32_t classify_min;     /* Proth/Riesel/Mersenne: index ranges at least this long walk only the
+                                  power-residue class of their zeros; 0 = 8192 */
+    uint32_t reserved;
 } ctd_tuning;
 
 /* Step forms a tuning can select.  AUTO: the fastest measured form for the
- * family and prime width.  WALK: the term-by-term walk (doubling and fixed-n
- * families: no baby-step blocks; Smarandache: the 64-bit Shoup step instead
- * of the 32-bit Barrett step).  MONTGOMERY: Smarandache steps in Montgomery
- * form (the general path).  Families without such a choice ignore it. */
+ * family and prime width.  WALK: the term-by-term walk (doubling families:
+ * no baby-step blocks and no power-residue classes; fixed-n families: the
+ * walk instead of the closed-form solve; Fibonacci/Lucas: no rank of
+ * apparition; Smarandache: the 64-bit Shoup step instead of the 32-bit
+ * Barrett step).  MONTGOMERY: Smarandache steps in Montgomery form (the
+ * general path).  Families without such a choice ignore it. */
 #define CTD_VARIANT_AUTO 0
 #define CTD_VARIANT_WALK 1
 #define CTD_VARIANT_MONTGOMERY 2
@@ -225,14 +229,17 @@ int ctd_serve_status(ctd_server *srv, uint32_t *active, uint32_t *queued, uint64
  * memory -- a process that reserves its whole memory budget at start-up and
  * admits work against it, or a host whose pool allocator owns all GPU
  * memory -- this is ctd_sieve_device without any cudaMalloc/cudaFree: its
- * scratch is a fixed array of about 8.6 MiB compiled into the library, held
- * on each GPU that loads the library until the process exits.  Limits:
+ * scratch is a fixed array of about 8.6 MiB compiled into the library.
+ * ctd_open places it on the context's device (it looks up the array's
+ * address, which loads it even under CUDA's lazy module loading), and it
+ * stays there until the process exits: reserve device memory after
+ * ctd_open, not before.  Limits:
  * hi - lo <= CTD_NOALLOC_SIEVE_MAX_RANGE and hi <= CTD_NOALLOC_SIEVE_MAX_HI;
  * larger requests return CTD_ERR_INVALID_ARGUMENT (message in
  * ctd_last_error).  Output as ctd_sieve_device: primes in [lo, hi) ascending
  * in the caller's d_out, *count the number of primes (synchronizes the
- * stream to read it).  The first call on a device looks up the array's
- * device address; make that first call before any stream capture.  All calls
+ * stream to read it).  Calls only read the address ctd_open looked up, so
+ * none of them does set-up work.  All calls
  * share the array: calls that overlap on the GPU (concurrent streams or
  * threads) race and must be serialized by the caller. */
 #define CTD_NOALLOC_SIEVE_MAX_RANGE (1ull << 26)

@@ -12,7 +12,9 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "libctd_oracle.so")
-REF_SRC = "/root/reference/src"
+# the reference checkout: $CTD_REFERENCE_ROOT, else /root/reference
+REF_ROOT = os.environ.get("CTD_REFERENCE_ROOT", "/root/reference")
+REF_SRC = os.path.join(REF_ROOT, "src")
 
 
 def build_oracle(verbose: bool = False) -> str:
@@ -37,7 +39,7 @@ def build_reference(verbose: bool = False) -> str | None:
     script = os.path.join(HERE, "build_ref.sh")
     out = os.path.join(HERE, "_ref", "cutrialdive_ref")
     try:
-        subprocess.check_call(["bash", script], stdout=None if verbose else subprocess.DEVNULL)
+        subprocess.check_call(["bash", script, REF_ROOT], stdout=None if verbose else subprocess.DEVNULL)
     except (subprocess.CalledProcessError, FileNotFoundError) as exc:  # pragma: no cover
         print(f"oracle/_ref: reference build failed: {exc}", file=sys.stderr)
         return None

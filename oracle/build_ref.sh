@@ -1,7 +1,8 @@
 #!/usr/bin/env bash
 # Builds the reference's own CPU trial-factoring engine (cutrialdive 1.2.0,
-# CPU build) from its unmodified sources under /root/reference/src into
-# oracle/_ref/cutrialdive_ref.  Test infrastructure only: it pins the oracle
+# CPU build) from its unmodified sources into oracle/_ref/cutrialdive_ref.
+# The reference checkout is the first argument, else $CTD_REFERENCE_ROOT,
+# else /root/reference.  Test infrastructure only: it pins the oracle
 # and produces the committed golden factor files; nothing in the product
 # loads it.
 #
@@ -14,7 +15,8 @@
 # are not compiled.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-SRC=/root/reference/src
+REF_ROOT="${1:-${CTD_REFERENCE_ROOT:-/root/reference}}"
+SRC="$REF_ROOT/src"
 OUT="$HERE/_ref"
 OBJ="$OUT/obj"
 [ -d "$SRC" ] || { echo "reference sources not found at $SRC" >&2; exit 1; }

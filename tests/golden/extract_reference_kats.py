@@ -186,7 +186,7 @@ def extract(ref_root: str) -> dict:
 
 
 if __name__ == "__main__":
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CTD_REFERENCE_ROOT", "/root/reference")
     data = extract(root)
     out = os.path.join(HERE, "reference_kats.json")
     with open(out, "w") as fh:

@@ -1,0 +1,20 @@
+// Host-side check of the doubling families' power-residue classes
+// (ctd_powres.cuh is __host__ __device__).  Reads "p wt" lines on stdin
+// (odd prime p, 0 < wt < p) and prints "M r": every n with 2^-n = wt (mod p)
+// satisfies n = r (mod M); M = 0 when no n does.
+#include <cinttypes>
+#include <cstdio>
+
+#include "../cutrialdive_gb300/csrc/ctd_powres.cuh"
+
+int main()
+{
+    unsigned long long p, wt;
+    while (std::scanf("%llu %llu", &p, &wt) == 2) {
+        ctd::Mont m;
+        m.init(p);
+        const ctd::PowerClass c = ctd::doubling_class(m, m.to(wt));
+        std::printf("%u %u\n", c.M, c.r);
+    }
+    return 0;
+}

@@ -66,6 +66,18 @@ def test_empty_ranges_are_reported_not_run():
     assert r.returncode == 0 and "Range [9, 9[ is empty, no prime numbers to divide by..." in r.stdout
 
 
+def test_unwritable_output_directory_fails_before_any_work(tmp_path):
+    """An output file that cannot be created stops the run with exit code 1
+    before the device is touched.  (The reference opens the file without
+    checking it and, exiting 0, writes the results nowhere; a drop-in should
+    not lose a run's results silently.)"""
+    out = tmp_path / "no_such_dir" / "factors.txt"
+    r = cli("--num-seq", "proth,3", "-s", "1", "-e", "100", "--tf-bits", "20", "--output", out)
+    assert r.returncode == 1
+    assert f"cannot open file {out}" in r.stderr + r.stdout
+    assert not out.parent.exists()
+
+
 def test_print_expression():
     # tests/smarandache_tests.cpp:311-324 and the per-family printers
     out = lambda *a: cli(*a).stdout.strip()  # noqa: E731

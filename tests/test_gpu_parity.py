@@ -167,20 +167,6 @@ def test_overflow_semantics_tribonacci_n1(eng):
             assert len(set(gl[i])) == m and set(gl[i]) <= primes
 
 
-def test_hits_divide_terms_at_scale(eng):
-    """Headline-sized slice (Proth 3*2^n+1, n < 100001, 2^28 primes above
-    2^32): every reported (n, p) divides S(n), checked with Python integers,
-    and the hit count matches the oracle on a sub-slice."""
-    f0, f1 = 1 << 32, (1 << 32) + (1 << 28)
-    got = run_gpu(eng, O.PROTH, 3, 1, 100001, f0, f1)
-    res = got.to_factoring_results()
-    hits = [(1 + i, p) for i in range(len(res)) for p in res[i]]
-    assert hits, "expected some factors"
-    for n, p in hits:
-        assert (3 * pow(2, n, p) + 1) % p == 0
-        assert f0 <= p < f1
-
-
 @pytest.mark.parametrize("family,n0,n1", [(O.FIBONACCI, 1, 2501), (O.LUCAS, 3, 1003), (O.TRIBONACCI, 2, 1502),
                                           (O.FIBONACCI, 7, 40)])
 def test_linear_recurrences_across_the_lazy_block_limit(eng, family, n0, n1):
@@ -203,3 +189,82 @@ def test_baby_step_blocks_tail_and_short_ranges(eng, family, param):
         got = run_gpu(eng, family, param, n0, n1, f0, f1)
         want = O.trial_factor(family, param, n0, n1, f0, f1, max_factors=32)
         assert text(got) == want.format(), (n0, n1)
+
+
+def test_two_contexts_sieve_and_run(eng):
+    """A second context on the same device (a device switch in between) sieves
+    and runs like the first: per-device kernel attributes are set per call."""
+    import torch
+
+    other = ctd.Engine(0)
+    try:
+        lo, hi = (1 << 33) + 12345, (1 << 33) + (1 << 22)
+        torch.cuda.set_device(0)
+        assert np.array_equal(other.sieve(lo, hi), eng.sieve(lo, hi))
+        a = run_gpu(other, O.PROTH, 3, 1, 5001, lo, hi)
+        b = run_gpu(eng, O.PROTH, 3, 1, 5001, lo, hi)
+        assert text(a) == text(b)
+    finally:
+        other.close()
+
+
+# ------------------------------------------- power-residue classes, fixed-n solve
+DOUBLING = [(O.PROTH, 3), (O.PROTH, 2718281828459), (O.RIESEL, 999_999), (O.RIESEL, 1), (O.MERSENNE, 0),
+            (O.PROTH, 1 << 20), (O.RIESEL, 3 * 5 * 7 * 11 * 13)]
+
+
+@pytest.mark.parametrize("family,param", DOUBLING)
+@pytest.mark.parametrize("f0,f1", [(0, 1 << 16), ((1 << 31) - (1 << 17), (1 << 31) + (1 << 17)),
+                                   ((1 << 40) + (1 << 30), (1 << 40) + (1 << 30) + (1 << 16))])
+def test_doubling_classes_vs_oracle(eng, family, param, f0, f1):
+    """Index ranges long enough for the power-residue classes (12000 terms):
+    small primes with dense hits, primes around 2^31 and above 2^40."""
+    n0, n1 = 5, 12005
+    got = run_gpu(eng, family, param, n0, n1, f0, f1, max_factors=64)
+    want = O.trial_factor(family, param, n0, n1, f0, f1, max_factors=64)
+    assert text(got) == want.format()
+
+
+@pytest.mark.parametrize("family,param", DOUBLING[:5])
+def test_doubling_classes_on_short_ranges(eng, family, param):
+    """The classified walk forced onto ranges of 1..300 terms (classes with
+    fewer terms than two blocks, partial blocks, the tail)."""
+    t = eng.get_tuning(family)
+    t["classify_min"] = 1
+    eng.set_tuning(family, t)
+    try:
+        f0, f1 = (1 << 33), (1 << 33) + (1 << 18)
+        for n0, n1 in [(5, 6), (5, 40), (5, 69), (1000, 1063), (1000, 1300), (7, 2100)]:
+            got = run_gpu(eng, family, param, n0, n1, f0, f1)
+            want = O.trial_factor(family, param, n0, n1, f0, f1, max_factors=32)
+            assert text(got) == want.format(), (n0, n1)
+        got = run_gpu(eng, family, param, 3, 2503, 0, 1 << 14, max_factors=64)
+        want = O.trial_factor(family, param, 3, 2503, 0, 1 << 14, max_factors=64)
+        assert text(got) == want.format()
+    finally:
+        eng.set_tuning(family, None)
+
+
+@pytest.mark.parametrize("family,param,n0,n1,f0,f1", [
+    (O.RIESEL, 999_999, 1, 30001, 1 << 33, (1 << 33) + (1 << 27)),
+    (O.MERSENNE, 0, 10000, 60000, 1 << 35, (1 << 35) + (1 << 27)),
+    (O.PROTH, 1279, 20000, 40000, 1 << 38, (1 << 38) + (1 << 27)),
+    (O.PROTH_FIXED_N, 20000, 1, 50001, 1 << 31, (1 << 31) + (1 << 27)),
+    (O.RIESEL_FIXED_N, 1234, 1, 70001, 1 << 36, (1 << 36) + (1 << 27)),
+    (O.PROTH_FIXED_N, 7, 0, 30000, 0, 1 << 20),
+])
+def test_default_forms_against_the_walk(eng, family, param, n0, n1, f0, f1):
+    """Power-residue classes (doubling) and the closed-form solve (fixed n)
+    against the term-by-term walk on ranges too large for the CPU oracle."""
+    def run(variant):
+        eng.set_tuning(family, None)
+        t = eng.get_tuning(family)
+        t["variant"] = variant
+        eng.set_tuning(family, t)
+        try:
+            return text(run_gpu(eng, family, param, n0, n1, f0, f1, max_factors=64))
+        finally:
+            eng.set_tuning(family, None)
+
+    fast, walk = run(0), run(1)
+    assert fast == walk

@@ -132,3 +132,15 @@ def test_checkpoint_wrong_version_and_truncation(tmp_path):
     with pytest.raises(RuntimeError, match="Truncated"):
         ctd.load_checkpoint(path)
     assert ctd.load_checkpoint(str(tmp_path / "absent")) is None
+
+
+def test_checkpoint_into_missing_directory(tmp_path):
+    """A checkpoint that cannot be created fails with the reference's message
+    (src/checkpoint.cpp:181-184) instead of losing the state silently."""
+    spec = ctd.num_seq_spec(ctd.num_seq_id.mersenne)
+    opts = ctd.trial_factoring_options(1, 3, 0, 100, None, 2)
+    buf = ctd.factors_buffer.empty(1, 2, 2)
+    path = str(tmp_path / "no_such_dir" / "x.chkpnt")
+    with pytest.raises(RuntimeError, match=r"Could not create temporary file `.*no_such_dir/x\.chkpnt\.tmp_\d+'"):
+        ctd.write_checkpoint(path, spec, opts, 7, buf)
+    assert not os.path.exists(os.path.dirname(path))

@@ -1,0 +1,103 @@
+"""The doubling families' power-residue classes (ctd_powres.cuh), run on the
+host from the kernel's own source and checked with Python integers: every
+n with 2^-n = wt (mod p) -- a zero of k*2^n-+1 or 2^n-1 -- lies in the class
+n = r (mod M) the kernel walks, and a prime classed as dividing no term
+(M = 0) really divides none (wt is outside the subgroup generated by 2)."""
+import os
+import random
+import shutil
+import subprocess
+
+import pytest
+
+sympy = pytest.importorskip("sympy")
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module")
+def checker(tmp_path_factory):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    exe = str(tmp_path_factory.mktemp("powres") / "powres_host_check")
+    subprocess.check_call([nvcc, "-O2", "-std=c++17", "-o", exe, os.path.join(HERE, "powres_host_check.cu")])
+    return exe
+
+
+def classes(checker, cases):
+    inp = "".join(f"{p} {w}\n" for p, w in cases)
+    out = subprocess.run([checker], input=inp, capture_output=True, text=True, check=True).stdout.split("\n")
+    return [tuple(map(int, line.split())) for line in out[:len(cases)]]
+
+
+def primes_for_test():
+    rnd = random.Random(11)
+    ps = [3, 5, 7, 11, 13, 17, 31, 41, 43, 97, 113, 193, 211, 257, 421, 631, 641, 1009, 2017, 65537, 3 * 2**30 + 1,
+          15 * 2**27 + 1, 7 * 2**26 + 1, 2**31 - 1, 1000000007, 2**32 + 15]
+    # primes with p - 1 divisible by large powers of 2 and by 3 * 5 * 7
+    for m in (2**10 * 105, 2**8 * 105, 105, 64 * 3, 64 * 35):
+        k = rnd.randrange(1, 2**22)
+        while len([q for q in ps if q % m == 1]) < 8:
+            if sympy.isprime(k * m + 1):
+                ps.append(k * m + 1)
+            k += 1
+    while len(ps) < 260:
+        bits = rnd.choice((12, 17, 24, 31, 33, 34))
+        q = sympy.nextprime(rnd.getrandbits(bits) | (1 << (bits - 1)))
+        ps.append(int(q))
+    return ps
+
+
+def test_every_zero_lies_in_the_class(checker):
+    rnd = random.Random(3)
+    cases = []
+    for p in primes_for_test():
+        for w in {1, p - 1, p - 3 % p if p > 3 else 1, rnd.randrange(1, p), rnd.randrange(1, p)}:
+            if 0 < w < p:
+                cases.append((p, w))
+    got = classes(checker, cases)
+    skipped = 0
+    for (p, w), (M, r) in zip(cases, got):
+        h = pow(2, -1, p)
+        order = int(sympy.n_order(2, p))
+        member = pow(w, order, p) == 1  # w in <2^-1> = <2>
+        if M == 0:
+            assert not member, (p, w)
+            skipped += 1
+            continue
+        assert 0 <= r < M and order % M == 0, (p, w, M, r)
+        if member:
+            n = int(sympy.discrete_log(p, w, h))
+            assert pow(h, n, p) == w
+            assert n % M == r, (p, w, M, r, n)
+    assert skipped > 0
+
+
+def test_small_primes_exhaustively(checker):
+    """Every prime below 600 and every target: the class holds all zeros of
+    one full period, and M = 0 exactly when there are none."""
+    cases = [(p, w) for p in map(int, sympy.primerange(3, 600)) for w in range(1, p)]
+    got = classes(checker, cases)
+    for (p, w), (M, r) in zip(cases, got):
+        h = pow(2, -1, p)
+        order = int(sympy.n_order(2, p))
+        zeros = [n for n in range(order) if pow(h, n, p) == w]
+        if M == 0:
+            assert zeros == [], (p, w)
+        else:
+            assert all(n % M == r for n in zeros), (p, w, M, r, zeros)
+
+
+def test_class_keeps_a_small_fraction_of_terms(checker):
+    """Proth k = 3 (wt = -3) over primes near 2^33: the walked fraction,
+    sum of 1/M over primes with a class, is near 0.15 of the terms."""
+    rnd = random.Random(1)
+    ps = []
+    x = 2**33 + rnd.getrandbits(30)
+    while len(ps) < 3000:
+        x = int(sympy.nextprime(x))
+        ps.append(x)
+    got = classes(checker, [(p, p - 3) for p in ps])
+    frac = sum(1 / M for M, _ in got if M) / len(ps)
+    assert 0.10 < frac < 0.22, frac
