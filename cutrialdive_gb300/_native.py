@@ -64,6 +64,7 @@ SIGNATURES = {
     "ctd_mod2_device": (i32, [vp, ctypes.POINTER(CtdJob), vp, vp, vp]),
     "ctd_sieve_device_noalloc": (i32, [vp, u64, u64, vp, u64, p64, vp]),
     "ctd_batch_run": (i32, [vp, ctypes.POINTER(CtdJob), u32, ctypes.POINTER(p32), ctypes.POINTER(p64), u64, i32]),
+    "ctd_batch_graph_stats": (i32, [vp, p64, p64, p64]),
     "ctd_serve_open": (i32, [vp, u64, u32, u64, ctypes.POINTER(vp)]),
     "ctd_serve_close": (None, [vp]),
     "ctd_serve_submit": (i32, [vp, ctypes.POINTER(CtdJob), p64]),

@@ -381,6 +381,14 @@ class Engine:
                     "ctd_batch_run")
 
 
+    def batch_graph_stats(self) -> dict:
+        """Graphs ctd_batch_run instantiated, updated in place and replayed."""
+        a, b, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        self._check(self._L.ctd_batch_graph_stats(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
+                    "ctd_batch_graph_stats")
+        return {"instantiations": a.value, "updates": b.value, "replays": c.value}
+
+
 class Server:
     """Continuous-batching server over ctd_serve_* (one device context)."""
 

@@ -5,15 +5,22 @@
 // no batching or serving layer.  Here:
 //
 // * ctd_batch_run walks the union of the jobs' prime ranges segment by
-//   segment ("chunk-major"): each 2^k-aligned segment is sieved once and
-//   consumed by every job whose range covers it, with one batched residue
-//   launch per family present.  The whole schedule -- sieve, bounds and
-//   residue kernels of every segment -- is captured once into a CUDA graph
-//   and launched once; nothing waits on the host until the end.
-// * ctd_serve_* keeps a set of active jobs with per-job prime cursors on the
-//   device and advances all of them by one aligned segment per tick; jobs
-//   submitted while others run are admitted at the next tick as slots and
-//   the device-memory budget allow (continuous batching).
+//   segment ("chunk-major"): each aligned segment is sieved once and
+//   consumed by every job whose range covers it, in ONE persistent walk
+//   launch over (job, 32 primes, index tile) work items of every family
+//   (launch_batch, ctd_residue.cu).  The whole schedule -- sieves, class and
+//   plan kernels, walks -- is captured once into a CUDA graph; a later call
+//   with the same schedule replays it, one with the same shape updates the
+//   instantiated graph in place, and the device buffers stay with the
+//   context (grown, never freed per call).
+// * ctd_serve_* keeps a device job table with a progress cursor per job
+//   (advanced by the kernels), admits queued jobs by slots and a device
+//   memory budget (ctd_admission.h) while earlier ticks still run, and
+//   queues each tick's work without waiting for the previous one: ticks
+//   overlap with the host's admission and result handling, and a finished
+//   job's results travel back by an asynchronous copy the host collects
+//   when its event has completed.
+#include "ctd_admission.h"
 #include "ctd_internal.h"
 
 #include <algorithm>
@@ -48,71 +55,228 @@ uint64_t job_bytes(const ctd_job &j)
     return counts_bytes(j) + (j.n1 - j.n0) * (uint64_t)j.max_factors * sizeof(uint64_t);
 }
 
-JobView view_of(ctd_ctx *ctx, const ctd_job &j, uint32_t *counts, uint64_t *factors)
-{
-    JobView v{};
-    v.family = j.family;
-    v.tiles = 1;
-    ctd_tuning t{};
-    v.variant = ctd_get_tuning(ctx, j.family, &t) == CTD_OK ? t.variant : CTD_VARIANT_AUTO;
-    v.param = j.param;
-    v.n0 = j.n0;
-    v.n1 = j.n1;
-    v.tile_len = j.n1 - j.n0;
-    v.fb.counts = counts;
-    v.fb.factors = factors;
-    v.fb.max_factors = j.max_factors;
-    return v;
-}
-
 // odd-prime range of a job after the prime 2 is handled separately
 uint64_t odd_f0(const ctd_job &j) { return j.f0 <= 2 ? 3 : j.f0; }
 
-struct Launch {  // one batched launch of a segment
-    uint32_t family;
-    uint32_t first;  // offset into the active-list array
-    uint32_t count;
-};
+bool is_doubling(uint32_t f) { return f == CTD_PROTH || f == CTD_RIESEL || f == CTD_MERSENNE; }
 
-struct Segment {
-    uint64_t lo, hi;
-    std::vector<Launch> launches;
-};
-
-int grid_for_family(ctd_ctx *ctx, uint32_t family)
+// Index tiles of a batched job: the longest units a warp item may take.
+// Smarandache terms cost ~11 integer instructions and the walk of each tile
+// starts with an O(log n) jump, so its ranges are cut at 4096 terms;
+// tribonacci at 16384; the rank-of-apparition (Fibonacci, Lucas) and
+// closed-form (fixed-n) paths depend on the whole range and stay whole; the
+// doubling walks are cut at 32768 terms of the full range.
+uint64_t tile_limit(uint32_t family)
 {
-    int per_sm = batch_blocks_per_sm(family);
-    return ctx_sm_count(ctx) * (per_sm > 0 ? per_sm : 1);
+    switch (family) {
+    case CTD_SMARANDACHE: return 4096;
+    case CTD_TRIBONACCI: return 16384;
+    case CTD_PROTH:
+    case CTD_RIESEL:
+    case CTD_MERSENNE: return 32768;
+    default: return ~0ull;
+    }
 }
+
+// relative cost of one term, for ordering a segment's jobs heaviest first
+double term_cost(uint32_t family)
+{
+    switch (family) {
+    case CTD_SMARANDACHE: return 11.0;
+    case CTD_TRIBONACCI: return 3.2;
+    case CTD_FIBONACCI:
+    case CTD_LUCAS: return 0.5;
+    case CTD_PROTH:
+    case CTD_RIESEL:
+    case CTD_MERSENNE: return 0.2;
+    default: return 0.01;
+    }
+}
+
+BatchJob batch_job_of(ctd_ctx *ctx, const ctd_job &j, uint32_t *counts, uint64_t *factors)
+{
+    BatchJob b{};
+    JobView &v = b.view;
+    const ctd_tuning t = ctx_tuning(ctx, j.family);
+    v.family = j.family;
+    v.variant = t.variant;
+    v.classify_min = t.classify_min ? t.classify_min : DEFAULT_CLASSIFY_MIN;
+    v.param = j.param;
+    v.n0 = j.n0;
+    v.n1 = j.n1;
+    const uint64_t N = j.n1 - j.n0;
+    const uint64_t lim = tile_limit(j.family);
+    v.tiles = (uint32_t)(N <= lim ? 1 : std::min<uint64_t>((N + lim - 1) / lim, 1u << 20));
+    v.tile_len = (N + v.tiles - 1) / v.tiles;
+    v.tiles = (uint32_t)((N + v.tile_len - 1) / v.tile_len);
+    v.fb.counts = counts;
+    v.fb.factors = factors;
+    v.fb.max_factors = j.max_factors;
+    b.f0 = odd_f0(j);
+    b.f1 = j.f1;
+    b.cursor = b.f0;
+    b.classified = is_doubling(j.family) && v.variant == CTD_VARIANT_AUTO && N >= v.classify_min;
+    return b;
+}
+
+template <class T>
+cudaError_t grow(T *&p, size_t &cap, size_t n)
+{
+    if (n <= cap && p)
+        return cudaSuccess;
+    cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc(&p, (n ? n : 1) * sizeof(T));
+    if (e == cudaSuccess)
+        cap = n;
+    return e;
+}
+
+// FNV-1a, for the key of a captured schedule
+struct Hasher {
+    uint64_t h = 1469598103934665603ull;
+    template <class T>
+    void add(const T &x)
+    {
+        const unsigned char *b = reinterpret_cast<const unsigned char *>(&x);
+        for (size_t i = 0; i < sizeof(T); ++i) {
+            h ^= b[i];
+            h *= 1099511628211ull;
+        }
+    }
+};
 
 }  // namespace
 
-struct ctd_server {
-    ctd_ctx *ctx = nullptr;
-    uint64_t budget = 0;
-    uint64_t used = 0;
-    uint32_t max_active = 0;
-    uint64_t seg = 0;
-    uint64_t next_id = 1;
-    struct Job {
-        uint64_t id;
-        ctd_job job;
-        uint32_t *d_counts = nullptr;
-        uint64_t *d_factors = nullptr;
-        uint64_t cursor = 0;  // next prime bound to process
-        std::chrono::steady_clock::time_point submitted;
-    };
-    std::deque<Job> queue;           // submitted, not admitted
-    std::vector<Job> active;
-    std::map<uint64_t, std::pair<std::vector<uint32_t>, std::vector<uint64_t>>> done;
-    // device scratch
-    uint64_t *d_primes = nullptr;
-    uint64_t primes_cap = 0;
-    BatchJob *d_jobs = nullptr;
-    uint32_t *d_active = nullptr;
-    BatchSpan *d_spans = nullptr;
-    uint32_t cap_jobs = 0;
+namespace ctd {
+
+// Device buffers of the batched runner, kept across calls, and the
+// instantiated graph of the last schedule with its key.
+struct BatchCache {
+    unsigned char *fb = nullptr;
+    size_t fb_cap = 0;
+    BatchJob *jobs = nullptr;
+    size_t jobs_cap = 0;
+    uint32_t *active = nullptr;
+    size_t active_cap = 0;
+    uint64_t *primes = nullptr;
+    size_t primes_cap = 0;
+    BatchSpan *spans = nullptr;
+    size_t spans_cap = 0;
+    BatchControl *ctl = nullptr;
+    size_t ctl_cap = 0;
+    uint32_t *codes = nullptr;
+    size_t codes_cap = 0;
+    ClassItem *items = nullptr;
+    size_t items_cap = 0;
+    uint32_t *bucket = nullptr;  // counts, cursors, bases: 3 x nactive x CLASS_BUCKETS
+    size_t bucket_cap = 0;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t key = 0;
+    uint64_t replays = 0, updates = 0, instantiations = 0;
+
+    BatchScratch scratch(uint32_t nactive) const
+    {
+        BatchScratch s;
+        s.spans = spans;
+        s.ctl = ctl;
+        s.codes = codes;
+        s.items = items;
+        s.bucket_count = bucket;
+        s.bucket_base = bucket + 2ull * nactive * CLASS_BUCKETS;
+        return s;
+    }
 };
+
+void batch_cache_destroy(BatchCache *bc)
+{
+    if (!bc)
+        return;
+    if (bc->exec)
+        cudaGraphExecDestroy(bc->exec);
+    cudaFree(bc->fb);
+    cudaFree(bc->jobs);
+    cudaFree(bc->active);
+    cudaFree(bc->primes);
+    cudaFree(bc->spans);
+    cudaFree(bc->ctl);
+    cudaFree(bc->codes);
+    cudaFree(bc->items);
+    cudaFree(bc->bucket);
+    delete bc;
+}
+
+}  // namespace ctd
+
+namespace {
+
+// One segment of a schedule: its range and its active jobs (a slice of the
+// concatenated active list), heaviest first.
+struct Segment {
+    uint64_t lo, hi;
+    uint32_t first, count;
+    bool any_classified;
+};
+
+// The segments of [lo, hi) aligned to S that some job covers, and their
+// active jobs; also the largest per-segment needs for sizing scratch.
+struct Schedule {
+    std::vector<Segment> segs;
+    std::vector<uint32_t> active;
+    uint64_t primes_cap = 0;
+    uint64_t class_cap = 0;
+    uint32_t max_active = 1;
+};
+
+Schedule plan_schedule(const std::vector<BatchJob> &hjobs, const ctd_job *jobs, uint64_t S)
+{
+    Schedule sc;
+    uint64_t lo = ~0ull, hi = 0;
+    for (const BatchJob &b : hjobs)
+        if (b.f0 < b.f1) {
+            lo = std::min(lo, b.f0);
+            hi = std::max(hi, b.f1);
+        }
+    if (lo >= hi)
+        return sc;
+    for (uint64_t k = lo / S; k * S < hi && k <= (~0ull / S); ++k) {
+        Segment sg;
+        sg.lo = std::max(k * S, lo);
+        sg.hi = (k + 1 > ~0ull / S) ? hi : std::min((k + 1) * S, hi);
+        std::vector<uint32_t> act;
+        uint64_t ncls = 0;
+        for (uint32_t i = 0; i < hjobs.size(); ++i)
+            if (hjobs[i].f0 < sg.hi && hjobs[i].f1 > sg.lo) {
+                act.push_back(i);
+                if (hjobs[i].classified)
+                    ncls += prime_count_upper_bound(std::max(sg.lo, hjobs[i].f0), std::min(sg.hi, hjobs[i].f1));
+            }
+        if (act.empty())
+            continue;
+        // heaviest work per prime first: the walk hands out items in this order
+        std::stable_sort(act.begin(), act.end(), [&](uint32_t x, uint32_t y) {
+            return (double)(jobs[x].n1 - jobs[x].n0) * term_cost(jobs[x].family) >
+                   (double)(jobs[y].n1 - jobs[y].n0) * term_cost(jobs[y].family);
+        });
+        for (size_t b = 0; b < act.size(); b += MAX_ACTIVE_PER_LAUNCH) {
+            Segment part = sg;
+            part.first = (uint32_t)sc.active.size();
+            part.count = (uint32_t)std::min<size_t>(MAX_ACTIVE_PER_LAUNCH, act.size() - b);
+            part.any_classified = false;
+            for (uint32_t q = 0; q < part.count; ++q)
+                part.any_classified |= hjobs[act[b + q]].classified != 0;
+            sc.active.insert(sc.active.end(), act.begin() + b, act.begin() + b + part.count);
+            sc.max_active = std::max(sc.max_active, part.count);
+            sc.segs.push_back(part);
+        }
+        sc.primes_cap = std::max(sc.primes_cap, prime_count_upper_bound(sg.lo, sg.hi));
+        sc.class_cap = std::max(sc.class_cap, ncls);
+    }
+    return sc;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -131,179 +295,270 @@ int ctd_batch_run(ctd_ctx *ctx, const ctd_job *jobs, uint32_t njobs, uint32_t *c
     CTX_TRY(cudaSetDevice(ctx_device(ctx)));
     cudaStream_t st = ctx_stream(ctx);
     std::string err;
-    int rc = CTD_OK;
+    BatchCache *&bcref = ctx_batch_cache(ctx);
+    if (!bcref) {
+        bcref = new (std::nothrow) BatchCache();
+        if (!bcref)
+            return ctx_fail(ctx, CTD_ERR_OUT_OF_MEMORY, "ctd_batch_run: host allocation");
+    }
+    BatchCache &bc = *bcref;
 
-    // device factors buffers, one allocation
+    // factors buffers: one region, grown across calls
     std::vector<uint64_t> off(njobs + 1, 0);
     for (uint32_t i = 0; i < njobs; ++i)
         off[i + 1] = off[i] + job_bytes(jobs[i]);
-    unsigned char *d_buf = nullptr;
-    BatchJob *d_jobs = nullptr;
-    uint32_t *d_active = nullptr;
-    BatchSpan *d_spans = nullptr;
-    uint64_t *d_primes = nullptr;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
+    CTX_TRY(grow(bc.fb, bc.fb_cap, off[njobs]));
     std::vector<BatchJob> hjobs(njobs);
-    std::vector<Segment> segs;
-    std::vector<uint32_t> hactive;
-    uint64_t lo = ~0ull, hi = 0, primes_cap = 0;
-    uint32_t max_launch = 1;
-
-    auto cleanup = [&]() {
-        if (exec)
-            cudaGraphExecDestroy(exec);
-        if (graph)
-            cudaGraphDestroy(graph);
-        cudaFree(d_buf);
-        cudaFree(d_jobs);
-        cudaFree(d_active);
-        cudaFree(d_spans);
-        cudaFree(d_primes);
-    };
-#define BATCH_TRY(expr)                                                                                   \
-    do {                                                                                                  \
-        cudaError_t e_ = (expr);                                                                          \
-        if (e_ != cudaSuccess) {                                                                          \
-            cleanup();                                                                                    \
-            return ctx_fail(ctx, e_ == cudaErrorMemoryAllocation ? CTD_ERR_OUT_OF_MEMORY : CTD_ERR_CUDA, \
-                            std::string(#expr ": ") + cudaGetErrorString(e_));                            \
-        }                                                                                                 \
-    } while (0)
-
-    BATCH_TRY(cudaMalloc(&d_buf, off[njobs]));
     for (uint32_t i = 0; i < njobs; ++i) {
-        const ctd_job &j = jobs[i];
-        const uint64_t N = j.n1 - j.n0;
-        auto *dc = reinterpret_cast<uint32_t *>(d_buf + off[i]);
-        auto *df = reinterpret_cast<uint64_t *>(d_buf + off[i] + counts_bytes(j));
-        BATCH_TRY(cudaMemcpyAsync(dc, counts_inout[i], N * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-        BATCH_TRY(cudaMemcpyAsync(df, factors_inout[i], N * j.max_factors * sizeof(uint64_t),
-                                  cudaMemcpyHostToDevice, st));
-        hjobs[i].view = view_of(ctx, j, dc, df);
-        hjobs[i].f0 = odd_f0(j);
-        hjobs[i].f1 = j.f1;
-        if (j.f0 <= 2 && j.f1 > 2) {  // the prime 2 for this job
-            rc = launch_mod2(hjobs[i].view, st, err);
-            if (rc) {
-                cleanup();
-                return ctx_fail(ctx, rc, err);
-            }
-        }
-        if (hjobs[i].f0 < hjobs[i].f1) {
-            lo = std::min(lo, hjobs[i].f0);
-            hi = std::max(hi, hjobs[i].f1);
-        }
+        auto *dc = reinterpret_cast<uint32_t *>(bc.fb + off[i]);
+        auto *df = reinterpret_cast<uint64_t *>(bc.fb + off[i] + counts_bytes(jobs[i]));
+        hjobs[i] = batch_job_of(ctx, jobs[i], dc, df);
     }
-    BATCH_TRY(cudaMalloc(&d_jobs, njobs * sizeof(BatchJob)));
-    BATCH_TRY(cudaMemcpyAsync(d_jobs, hjobs.data(), njobs * sizeof(BatchJob), cudaMemcpyHostToDevice, st));
-
-    // chunk-major schedule over aligned segments
-    if (lo < hi) {
-        for (uint64_t k = lo / S; k * S < hi && k <= (~0ull / S); ++k) {
-            Segment sg;
-            sg.lo = std::max(k * S, lo);
-            sg.hi = (k + 1 > ~0ull / S) ? hi : std::min((k + 1) * S, hi);
-            std::map<uint32_t, std::vector<uint32_t>> byfam;
-            for (uint32_t i = 0; i < njobs; ++i)
-                if (hjobs[i].f0 < sg.hi && hjobs[i].f1 > sg.lo)
-                    byfam[jobs[i].family].push_back(i);
-            if (byfam.empty())
-                continue;
-            for (auto &kv : byfam) {
-                // longest index range first (the kernel hands out items in this order)
-                std::stable_sort(kv.second.begin(), kv.second.end(), [&](uint32_t x, uint32_t y) {
-                    return jobs[x].n1 - jobs[x].n0 > jobs[y].n1 - jobs[y].n0;
-                });
-                for (size_t b = 0; b < kv.second.size(); b += MAX_ACTIVE_PER_LAUNCH) {
-                    Launch l;
-                    l.family = kv.first;
-                    l.first = (uint32_t)hactive.size();
-                    l.count = (uint32_t)std::min<size_t>(MAX_ACTIVE_PER_LAUNCH, kv.second.size() - b);
-                    hactive.insert(hactive.end(), kv.second.begin() + b, kv.second.begin() + b + l.count);
-                    max_launch = std::max(max_launch, l.count);
-                    sg.launches.push_back(l);
-                }
-            }
-            primes_cap = std::max(primes_cap, prime_count_upper_bound(sg.lo, sg.hi));
-            segs.push_back(std::move(sg));
-        }
-    }
-    if (!segs.empty()) {
-        BATCH_TRY(cudaMalloc(&d_active, hactive.size() * sizeof(uint32_t)));
-        BATCH_TRY(cudaMemcpyAsync(d_active, hactive.data(), hactive.size() * sizeof(uint32_t),
-                                  cudaMemcpyHostToDevice, st));
-        BATCH_TRY(cudaMalloc(&d_spans, (max_launch + 1) * sizeof(BatchSpan)));
-        BATCH_TRY(cudaMalloc(&d_primes, primes_cap * sizeof(uint64_t)));
-        rc = sieve_prepare_base(ctx_workspace(ctx), hi, st, err);
+    const Schedule sc = plan_schedule(hjobs, jobs, S);
+    CTX_TRY(grow(bc.jobs, bc.jobs_cap, njobs));
+    CTX_TRY(grow(bc.active, bc.active_cap, std::max<size_t>(sc.active.size(), 1)));
+    CTX_TRY(grow(bc.primes, bc.primes_cap, std::max<uint64_t>(sc.primes_cap, 1)));
+    CTX_TRY(grow(bc.spans, bc.spans_cap, sc.max_active + 1));
+    CTX_TRY(grow(bc.ctl, bc.ctl_cap, 1));
+    CTX_TRY(grow(bc.codes, bc.codes_cap, std::max<uint64_t>(sc.class_cap, 1)));
+    CTX_TRY(grow(bc.items, bc.items_cap, std::max<uint64_t>(sc.class_cap, 1)));
+    CTX_TRY(grow(bc.bucket, bc.bucket_cap, 3ull * sc.max_active * CLASS_BUCKETS));
+    if (!sc.segs.empty()) {
+        uint64_t hi = 0;
+        for (const Segment &g : sc.segs)
+            hi = std::max(hi, g.hi);
+        int rc = sieve_prepare_base(ctx_workspace(ctx), hi, st, err);
         if (!rc)
             rc = sieve_prepare_windows(ctx_workspace(ctx), S, err);
-        if (rc) {
-            cleanup();
+        if (rc)
             return ctx_fail(ctx, rc, err);
-        }
-        BATCH_TRY(cudaStreamSynchronize(st));
-        std::vector<int> grids(CTD_PEANO + 1, 0);
-        for (auto &sg : segs)
-            for (auto &l : sg.launches)
-                if (!grids[l.family])
-                    grids[l.family] = grid_for_family(ctx, l.family);
-        if (use_graph)
-            BATCH_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        for (auto &sg : segs) {
-            const uint64_t *d_count = nullptr;
-            rc = sieve_odd_async(ctx_workspace(ctx), sg.lo, sg.hi, d_primes, primes_cap, &d_count, st, err);
-            for (size_t li = 0; !rc && li < sg.launches.size(); ++li) {
-                const Launch &l = sg.launches[li];
-                rc = launch_batch(l.family, d_jobs, d_active + l.first, l.count, d_primes, d_count, sg.lo, sg.hi,
-                                  d_spans, grids[l.family], st, err);
+    }
+
+    // inputs of this call: resume states, job table (cursors reset), active lists
+    for (uint32_t i = 0; i < njobs; ++i) {
+        const ctd_job &j = jobs[i];
+        const uint64_t N = j.n1 - j.n0;
+        CTX_TRY(cudaMemcpyAsync(hjobs[i].view.fb.counts, counts_inout[i], N * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                st));
+        CTX_TRY(cudaMemcpyAsync(hjobs[i].view.fb.factors, factors_inout[i], N * j.max_factors * sizeof(uint64_t),
+                                cudaMemcpyHostToDevice, st));
+    }
+    CTX_TRY(cudaMemcpyAsync(bc.jobs, hjobs.data(), njobs * sizeof(BatchJob), cudaMemcpyHostToDevice, st));
+    if (!sc.active.empty())
+        CTX_TRY(cudaMemcpyAsync(bc.active, sc.active.data(), sc.active.size() * sizeof(uint32_t),
+                                cudaMemcpyHostToDevice, st));
+
+    // the schedule: the prime 2 of the jobs that include it, then per segment
+    // the sieve and one batched launch
+    auto enqueue = [&]() -> int {
+        for (uint32_t i = 0; i < njobs; ++i)
+            if (jobs[i].f0 <= 2 && jobs[i].f1 > 2) {
+                int rc = launch_mod2(hjobs[i].view, st, err);
+                if (rc)
+                    return rc;
             }
+        for (const Segment &g : sc.segs) {
+            const uint64_t *d_count = nullptr;
+            int rc = sieve_odd_async(ctx_workspace(ctx), g.lo, g.hi, bc.primes, bc.primes_cap, &d_count, st, err);
+            if (!rc)
+                rc = launch_batch(bc.jobs, bc.active + g.first, g.count, g.any_classified, bc.primes, d_count, g.lo,
+                                  g.hi, bc.scratch(g.count), ctx_sm_count(ctx), st, err);
             if (rc)
-                break;
+                return rc;
         }
-        if (use_graph) {
+        return CTD_OK;
+    };
+    if (!use_graph) {
+        int rc = enqueue();
+        if (rc)
+            return ctx_fail(ctx, rc, err);
+    } else {
+        // the key: every argument the captured launches take
+        Hasher h;
+        h.add(sieve_state_key(ctx_workspace(ctx)));
+        h.add(ctx_sm_count(ctx));
+        for (const void *p : {(const void *)bc.fb, (const void *)bc.jobs, (const void *)bc.active,
+                              (const void *)bc.primes, (const void *)bc.spans, (const void *)bc.ctl,
+                              (const void *)bc.codes, (const void *)bc.items, (const void *)bc.bucket})
+            h.add(p);
+        h.add(bc.primes_cap);
+        for (uint32_t i = 0; i < njobs; ++i)
+            if (jobs[i].f0 <= 2 && jobs[i].f1 > 2)
+                h.add(hjobs[i].view);
+        for (const Segment &g : sc.segs) {
+            h.add(g.lo);
+            h.add(g.hi);
+            h.add(g.first);
+            h.add(g.count);
+            h.add(g.any_classified);
+        }
+        if (!bc.exec || bc.key != h.h) {
+            cudaGraph_t graph = nullptr;
+            CTX_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            int rc = enqueue();
             cudaError_t e = cudaStreamEndCapture(st, &graph);
             if (rc) {
-                cleanup();
+                if (graph)
+                    cudaGraphDestroy(graph);
                 return ctx_fail(ctx, rc, err);
             }
-            BATCH_TRY(e);
-            BATCH_TRY(cudaGraphInstantiate(&exec, graph, 0));
-            BATCH_TRY(cudaGraphLaunch(exec, st));
-        } else if (rc) {
-            cleanup();
-            return ctx_fail(ctx, rc, err);
+            CTX_TRY(e);
+            bool updated = false;
+            if (bc.exec) {
+                cudaGraphExecUpdateResultInfo info;
+                updated = cudaGraphExecUpdate(bc.exec, graph, &info) == cudaSuccess;
+                if (!updated) {
+                    cudaGetLastError();  // clear the update's error
+                    cudaGraphExecDestroy(bc.exec);
+                    bc.exec = nullptr;
+                }
+            }
+            if (!updated) {
+                e = cudaGraphInstantiate(&bc.exec, graph, 0);
+                if (e != cudaSuccess) {
+                    cudaGraphDestroy(graph);
+                    bc.exec = nullptr;
+                    CTX_TRY(e);
+                }
+                ++bc.instantiations;
+            } else {
+                ++bc.updates;
+            }
+            cudaGraphDestroy(graph);
+            bc.key = h.h;
+        } else {
+            ++bc.replays;
         }
+        CTX_TRY(cudaGraphLaunch(bc.exec, st));
     }
     for (uint32_t i = 0; i < njobs; ++i) {
         const ctd_job &j = jobs[i];
         const uint64_t N = j.n1 - j.n0;
-        BATCH_TRY(cudaMemcpyAsync(counts_inout[i], hjobs[i].view.fb.counts, N * sizeof(uint32_t),
-                                  cudaMemcpyDeviceToHost, st));
-        BATCH_TRY(cudaMemcpyAsync(factors_inout[i], hjobs[i].view.fb.factors, N * j.max_factors * sizeof(uint64_t),
-                                  cudaMemcpyDeviceToHost, st));
+        CTX_TRY(cudaMemcpyAsync(counts_inout[i], hjobs[i].view.fb.counts, N * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                st));
+        CTX_TRY(cudaMemcpyAsync(factors_inout[i], hjobs[i].view.fb.factors, N * j.max_factors * sizeof(uint64_t),
+                                cudaMemcpyDeviceToHost, st));
     }
-    BATCH_TRY(cudaStreamSynchronize(st));
-    cleanup();
-#undef BATCH_TRY
+    CTX_TRY(cudaStreamSynchronize(st));
     return CTD_OK;
 }
 
+int ctd_batch_graph_stats(ctd_ctx *ctx, uint64_t *instantiations, uint64_t *updates, uint64_t *replays)
+{
+    if (!ctx)
+        return CTD_ERR_INVALID_ARGUMENT;
+    const BatchCache *bc = ctx_batch_cache(ctx);
+    if (instantiations)
+        *instantiations = bc ? bc->instantiations : 0;
+    if (updates)
+        *updates = bc ? bc->updates : 0;
+    if (replays)
+        *replays = bc ? bc->replays : 0;
+    return CTD_OK;
+}
+
+}  // extern "C"
+
 // ------------------------------------------------------------ the server
+//
+// Slots: the device job table holds max_active entries; a job admitted into
+// a slot keeps it until its results are collected.  Each tick groups the
+// running jobs by the aligned segment their cursor is in (jobs in the same
+// segment share its sieve) and queues, per group, the sieve and one batched
+// launch; the kernels move each job's device cursor to the segment's end.
+// The host keeps the same cursor arithmetic to plan the next tick, so it
+// never reads the device between ticks.  At most TICKS_IN_FLIGHT ticks are
+// queued ahead of the GPU.
+
+struct ctd_server {
+    ctd_ctx *ctx = nullptr;
+    uint64_t seg = 0;
+    uint64_t next_id = 1;
+    struct Job {
+        uint64_t id = 0;
+        ctd_job job{};
+        uint32_t slot = 0;
+        uint32_t *d_counts = nullptr;
+        uint64_t *d_factors = nullptr;
+        uint64_t cursor = 0;  // host mirror of the device cursor
+        bool finishing = false;
+        cudaEvent_t done_event = nullptr;
+        uint32_t *h_counts = nullptr;  // pinned, filled by the final copy
+        uint64_t *h_factors = nullptr;
+    };
+    Admission<Job> adm;
+    std::vector<Job> running;  // admitted, not yet collected
+    std::vector<uint32_t> free_slots;
+    std::map<uint64_t, Job> done;
+    // device
+    BatchJob *d_jobs = nullptr;
+    uint32_t *d_active = nullptr;
+    uint64_t *d_primes = nullptr;
+    uint64_t primes_cap = 0;
+    BatchSpan *d_spans = nullptr;
+    BatchControl *d_ctl = nullptr;
+    uint32_t *d_codes = nullptr;
+    ClassItem *d_items = nullptr;
+    uint64_t class_cap = 0;
+    uint32_t *d_bucket = nullptr;
+    BatchJob *h_stage = nullptr;   // pinned staging for slot descriptors
+    uint32_t *h_active = nullptr;  // pinned active lists, one region per tick in flight
+    std::deque<cudaEvent_t> inflight;
+    uint64_t tick_count = 0;
+    static constexpr int TICKS_IN_FLIGHT = 2;
+};
+
+namespace {
+
+void free_job_host(ctd_server::Job &j)
+{
+    if (j.done_event)
+        cudaEventDestroy(j.done_event);
+    cudaFreeHost(j.h_counts);
+    cudaFreeHost(j.h_factors);
+    j.done_event = nullptr;
+    j.h_counts = nullptr;
+    j.h_factors = nullptr;
+}
+
+}  // namespace
+
+extern "C" {
 
 int ctd_serve_open(ctd_ctx *ctx, uint64_t memory_budget, uint32_t max_active, uint64_t segment_length,
                    ctd_server **out)
 {
-    if (!ctx || !out || !max_active)
+    if (!ctx || !out || !max_active || max_active > MAX_ACTIVE_PER_LAUNCH)
         return ctx ? ctx_fail(ctx, CTD_ERR_INVALID_ARGUMENT, "ctd_serve_open: bad arguments")
                    : CTD_ERR_INVALID_ARGUMENT;
+    CTX_TRY(cudaSetDevice(ctx_device(ctx)));
     auto *srv = new (std::nothrow) ctd_server();
     if (!srv)
         return CTD_ERR_OUT_OF_MEMORY;
     srv->ctx = ctx;
-    srv->budget = memory_budget;
-    srv->max_active = max_active;
+    srv->adm.budget = memory_budget;
+    srv->adm.max_active = max_active;
     srv->seg = segment_length ? segment_length : (1ull << 30);
+    cudaError_t e = cudaMalloc(&srv->d_jobs, max_active * sizeof(BatchJob));
+    if (e == cudaSuccess)
+        e = cudaMalloc(&srv->d_active, (size_t)ctd_server::TICKS_IN_FLIGHT * max_active * sizeof(uint32_t));
+    if (e == cudaSuccess)
+        e = cudaMalloc(&srv->d_spans, (max_active + 1) * sizeof(BatchSpan));
+    if (e == cudaSuccess)
+        e = cudaMalloc(&srv->d_ctl, sizeof(BatchControl));
+    if (e == cudaSuccess)
+        e = cudaMalloc(&srv->d_bucket, 3ull * max_active * CLASS_BUCKETS * sizeof(uint32_t));
+    if (e == cudaSuccess)
+        e = cudaMallocHost(&srv->h_stage, max_active * sizeof(BatchJob));
+    if (e == cudaSuccess)
+        e = cudaMallocHost(&srv->h_active, (size_t)ctd_server::TICKS_IN_FLIGHT * max_active * sizeof(uint32_t));
+    if (e != cudaSuccess) {
+        ctd_serve_close(srv);
+        return ctx_fail(ctx, e == cudaErrorMemoryAllocation ? CTD_ERR_OUT_OF_MEMORY : CTD_ERR_CUDA,
+                        std::string("ctd_serve_open: ") + cudaGetErrorString(e));
+    }
+    for (uint32_t s = max_active; s-- > 0;)
+        srv->free_slots.push_back(s);
     *out = srv;
     return CTD_OK;
 }
@@ -314,14 +569,25 @@ void ctd_serve_close(ctd_server *srv)
         return;
     cudaSetDevice(ctx_device(srv->ctx));
     cudaStreamSynchronize(ctx_stream(srv->ctx));
-    for (auto &j : srv->active) {
+    for (auto &j : srv->running) {
         cudaFree(j.d_counts);
         cudaFree(j.d_factors);
+        free_job_host(j);
     }
-    cudaFree(srv->d_primes);
+    for (auto &kv : srv->done)
+        free_job_host(kv.second);
+    for (cudaEvent_t ev : srv->inflight)
+        cudaEventDestroy(ev);
     cudaFree(srv->d_jobs);
     cudaFree(srv->d_active);
+    cudaFree(srv->d_primes);
     cudaFree(srv->d_spans);
+    cudaFree(srv->d_ctl);
+    cudaFree(srv->d_codes);
+    cudaFree(srv->d_items);
+    cudaFree(srv->d_bucket);
+    cudaFreeHost(srv->h_stage);
+    cudaFreeHost(srv->h_active);
     delete srv;
 }
 
@@ -334,8 +600,7 @@ int ctd_serve_submit(ctd_server *srv, const ctd_job *job, uint64_t *id)
     ctd_server::Job j;
     j.id = srv->next_id++;
     j.job = *job;
-    j.submitted = std::chrono::steady_clock::now();
-    srv->queue.push_back(j);
+    srv->adm.queue.push_back(j);
     *id = j.id;
     return CTD_OK;
 }
@@ -345,11 +610,11 @@ int ctd_serve_status(ctd_server *srv, uint32_t *active, uint32_t *queued, uint64
     if (!srv)
         return CTD_ERR_INVALID_ARGUMENT;
     if (active)
-        *active = (uint32_t)srv->active.size();
+        *active = srv->adm.active;
     if (queued)
-        *queued = (uint32_t)srv->queue.size();
+        *queued = (uint32_t)srv->adm.queue.size();
     if (memory_used)
-        *memory_used = srv->used;
+        *memory_used = srv->adm.used;
     return CTD_OK;
 }
 
@@ -362,146 +627,193 @@ int ctd_serve_tick(ctd_server *srv, uint64_t *done_ids, uint32_t cap, uint32_t *
     CTX_TRY(cudaSetDevice(ctx_device(ctx)));
     cudaStream_t st = ctx_stream(ctx);
     std::string err;
-    // admission: slots and the memory budget, in arrival order
-    while (!srv->queue.empty() && srv->active.size() < srv->max_active) {
-        ctd_server::Job &q = srv->queue.front();
-        const uint64_t bytes = job_bytes(q.job);
-        if (srv->used + bytes > srv->budget && !srv->active.empty())
-            break;
-        const uint64_t N = q.job.n1 - q.job.n0;
-        CTX_TRY(cudaMallocAsync(&q.d_counts, N * sizeof(uint32_t), st));
-        CTX_TRY(cudaMallocAsync(&q.d_factors, N * q.job.max_factors * sizeof(uint64_t), st));
-        CTX_TRY(cudaMemsetAsync(q.d_counts, 0, N * sizeof(uint32_t), st));
-        CTX_TRY(cudaMemsetAsync(q.d_factors, 0, N * q.job.max_factors * sizeof(uint64_t), st));
-        if (q.job.f0 <= 2 && q.job.f1 > 2) {
-            int rc = launch_mod2(view_of(ctx, q.job, q.d_counts, q.d_factors), st, err);
-            if (rc)
-                return ctx_fail(ctx, rc, err);
-        }
-        q.cursor = odd_f0(q.job);
-        srv->used += bytes;
-        srv->active.push_back(q);
-        srv->queue.pop_front();
-    }
-    if (srv->active.empty())
-        return CTD_OK;
-    // every active job advances over its current aligned segment; jobs on the
-    // same segment share its sieve
     const uint64_t S = srv->seg;
-    std::map<uint64_t, std::vector<uint32_t>> byseg;
-    for (uint32_t i = 0; i < srv->active.size(); ++i) {
-        auto &j = srv->active[i];
-        if (j.cursor < j.job.f1)
-            byseg[j.cursor / S].push_back(i);
-    }
-    const uint32_t na = (uint32_t)srv->active.size();
-    if (na > srv->cap_jobs) {
-        cudaFree(srv->d_jobs);
-        cudaFree(srv->d_active);
-        cudaFree(srv->d_spans);
-        srv->d_jobs = nullptr;
-        srv->d_active = nullptr;
-        srv->d_spans = nullptr;
-        srv->cap_jobs = 0;
-        CTX_TRY(cudaMalloc(&srv->d_jobs, na * sizeof(BatchJob)));
-        CTX_TRY(cudaMalloc(&srv->d_active, na * sizeof(uint32_t)));
-        CTX_TRY(cudaMalloc(&srv->d_spans, (na + 1) * sizeof(BatchSpan)));
-        srv->cap_jobs = na;
-    }
-    std::vector<BatchJob> hj(na);
-    for (uint32_t i = 0; i < na; ++i) {
-        auto &j = srv->active[i];
-        hj[i].view = view_of(ctx, j.job, j.d_counts, j.d_factors);
-        hj[i].f0 = odd_f0(j.job);
-        hj[i].f1 = j.job.f1;
-    }
-    CTX_TRY(cudaMemcpyAsync(srv->d_jobs, hj.data(), na * sizeof(BatchJob), cudaMemcpyHostToDevice, st));
-    // capacity for the primes of the largest segment group of this tick
-    uint64_t primes_need = 0;
-    for (auto &kv : byseg) {
-        const uint64_t slo = kv.first * S;
-        primes_need = std::max(primes_need, prime_count_upper_bound(slo, slo + S));
-    }
-    if (primes_need > srv->primes_cap) {
-        cudaFree(srv->d_primes);
-        srv->d_primes = nullptr;
-        srv->primes_cap = 0;
-        CTX_TRY(cudaMalloc(&srv->d_primes, primes_need * sizeof(uint64_t)));
-        srv->primes_cap = primes_need;
-    }
-    uint64_t maxhi = 0;
-    for (auto &j : srv->active)
-        maxhi = std::max(maxhi, j.job.f1);
-    int rc = sieve_prepare_base(ctx_workspace(ctx), maxhi, st, err);
-    if (!rc)
-        rc = sieve_prepare_windows(ctx_workspace(ctx), S, err);
-    if (rc)
-        return ctx_fail(ctx, rc, err);
-    std::vector<uint32_t> order;  // active indices grouped by segment then family
-    struct L { uint64_t lo, hi; uint32_t family, first, count; };
-    std::vector<L> launches;
-    for (auto &kv : byseg) {
-        uint64_t lo = ~0ull, hi = 0;
-        std::map<uint32_t, std::vector<uint32_t>> byfam;
-        for (uint32_t i : kv.second) {
-            auto &j = srv->active[i];
-            lo = std::min(lo, j.cursor);
-            hi = std::max(hi, std::min(j.job.f1, (kv.first + 1) * S));
-            byfam[j.job.family].push_back(i);
-        }
-        for (auto &f : byfam) {
-            // longest index range first (the kernel hands out items in this order)
-            std::stable_sort(f.second.begin(), f.second.end(), [&](uint32_t x, uint32_t y) {
-                const ctd_job &a = srv->active[x].job, &c = srv->active[y].job;
-                return a.n1 - a.n0 > c.n1 - c.n0;
-            });
-            launches.push_back({lo, hi, f.first, (uint32_t)order.size(), (uint32_t)f.second.size()});
-            order.insert(order.end(), f.second.begin(), f.second.end());
-        }
-    }
-    CTX_TRY(cudaMemcpyAsync(srv->d_active, order.data(), order.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-    // the launches of one segment follow its sieve; launches are grouped by segment
-    uint64_t cur_lo = ~0ull, cur_hi = 0;
-    const uint64_t *d_count = nullptr;
-    for (auto &l : launches) {
-        if (l.lo != cur_lo || l.hi != cur_hi) {
-            rc = sieve_odd_async(ctx_workspace(ctx), l.lo, l.hi, srv->d_primes, srv->primes_cap, &d_count, st, err);
-            if (rc)
-                return ctx_fail(ctx, rc, err);
-            cur_lo = l.lo;
-            cur_hi = l.hi;
-        }
-        rc = launch_batch(l.family, srv->d_jobs, srv->d_active + l.first, l.count, srv->d_primes, d_count, l.lo, l.hi,
-                          srv->d_spans, grid_for_family(ctx, l.family), st, err);
-        if (rc)
-            return ctx_fail(ctx, rc, err);
-    }
-    // advance cursors; finished jobs hand their results back to the host
-    std::vector<ctd_server::Job> still;
-    for (auto &j : srv->active) {
-        const uint64_t seg_end = (j.cursor / S + 1) * S;
-        const uint64_t upto = std::min(j.job.f1, seg_end);
-        j.cursor = upto;
-        if (j.cursor >= j.job.f1) {
-            const uint64_t N = j.job.n1 - j.job.n0;
-            auto &res = srv->done[j.id];
-            res.first.resize(N);
-            res.second.resize(N * j.job.max_factors);
-            CTX_TRY(cudaMemcpyAsync(res.first.data(), j.d_counts, N * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-            CTX_TRY(cudaMemcpyAsync(res.second.data(), j.d_factors, N * j.job.max_factors * sizeof(uint64_t),
-                                    cudaMemcpyDeviceToHost, st));
-            CTX_TRY(cudaFreeAsync(j.d_counts, st));
-            CTX_TRY(cudaFreeAsync(j.d_factors, st));
-            srv->used -= job_bytes(j.job);
+
+    // 1. collect finished jobs whose results have arrived on the host
+    for (size_t k = 0; k < srv->running.size();) {
+        ctd_server::Job &j = srv->running[k];
+        if (j.finishing && cudaEventQuery(j.done_event) == cudaSuccess) {
+            srv->adm.release(job_bytes(j.job));
+            srv->free_slots.push_back(j.slot);
             if (*ndone < cap)
                 done_ids[*ndone] = j.id;
             ++*ndone;
+            srv->done[j.id] = j;
+            srv->running.erase(srv->running.begin() + (long)k);
         } else {
-            still.push_back(j);
+            ++k;
         }
     }
-    CTX_TRY(cudaStreamSynchronize(st));
-    srv->active.swap(still);
+    cudaGetLastError();  // cudaEventQuery's "not ready" is not an error
+
+    // 2. admission: slots and the memory budget, arrival order
+    std::vector<ctd_server::Job> admitted;
+    int arc = srv->adm.admit(
+        [](const ctd_server::Job &j) { return job_bytes(j.job); },
+        [&](ctd_server::Job &j, uint64_t) -> int {
+            const uint64_t N = j.job.n1 - j.job.n0;
+            cudaError_t e = cudaMallocAsync(&j.d_counts, N * sizeof(uint32_t), st);
+            if (e == cudaSuccess)
+                e = cudaMallocAsync(&j.d_factors, N * j.job.max_factors * sizeof(uint64_t), st);
+            if (e != cudaSuccess) {
+                if (j.d_counts)
+                    cudaFreeAsync(j.d_counts, st);
+                j.d_counts = nullptr;
+                j.d_factors = nullptr;
+                cudaGetLastError();
+                err = std::string("job buffers: ") + cudaGetErrorString(e);
+                return CTD_ERR_OUT_OF_MEMORY;
+            }
+            return CTD_OK;
+        },
+        [&](ctd_server::Job &j) { admitted.push_back(j); });
+    for (ctd_server::Job &j : admitted) {
+        const uint64_t N = j.job.n1 - j.job.n0;
+        j.slot = srv->free_slots.back();
+        srv->free_slots.pop_back();
+        CTX_TRY(cudaMemsetAsync(j.d_counts, 0, N * sizeof(uint32_t), st));
+        CTX_TRY(cudaMemsetAsync(j.d_factors, 0, N * j.job.max_factors * sizeof(uint64_t), st));
+        BatchJob b = batch_job_of(ctx, j.job, j.d_counts, j.d_factors);
+        if (j.job.f0 <= 2 && j.job.f1 > 2) {
+            int rc = launch_mod2(b.view, st, err);
+            if (rc)
+                return ctx_fail(ctx, rc, err);
+        }
+        j.cursor = b.f0;
+        srv->h_stage[j.slot] = b;
+        CTX_TRY(cudaMemcpyAsync(srv->d_jobs + j.slot, srv->h_stage + j.slot, sizeof(BatchJob), cudaMemcpyHostToDevice,
+                                st));
+        srv->running.push_back(j);
+    }
+    if (arc && srv->running.empty())
+        return ctx_fail(ctx, arc, err);  // nothing runs and the first queued job cannot be placed
+
+    // 3. one tick: every running job advances over its cursor's segment
+    std::map<uint64_t, std::vector<uint32_t>> byseg;  // segment index -> running indices
+    for (uint32_t k = 0; k < srv->running.size(); ++k) {
+        const ctd_server::Job &j = srv->running[k];
+        if (!j.finishing && j.cursor < j.job.f1)
+            byseg[j.cursor / S].push_back(k);
+    }
+    if (!byseg.empty()) {
+        // bounded lead over the GPU: wait for the tick before last
+        while ((int)srv->inflight.size() >= ctd_server::TICKS_IN_FLIGHT) {
+            CTX_TRY(cudaEventSynchronize(srv->inflight.front()));
+            cudaEventDestroy(srv->inflight.front());
+            srv->inflight.pop_front();
+        }
+        uint64_t primes_need = 0, class_need = 0, maxhi = 0;
+        for (auto &kv : byseg) {
+            const uint64_t slo = kv.first * S;
+            primes_need = std::max(primes_need, prime_count_upper_bound(slo, slo + S));
+            uint64_t ncls = 0;
+            for (uint32_t k : kv.second) {
+                const ctd_server::Job &j = srv->running[k];
+                maxhi = std::max(maxhi, j.job.f1);
+                if (srv->h_stage[j.slot].classified)
+                    ncls += prime_count_upper_bound(std::max(slo, j.cursor), std::min(slo + S, j.job.f1));
+            }
+            class_need = std::max(class_need, ncls);
+        }
+        if (primes_need > srv->primes_cap || class_need > srv->class_cap) {
+            // regrow between ticks: everything queued so far must finish first
+            CTX_TRY(cudaStreamSynchronize(st));
+            if (primes_need > srv->primes_cap) {
+                cudaFree(srv->d_primes);
+                srv->d_primes = nullptr;
+                srv->primes_cap = 0;
+                CTX_TRY(cudaMalloc(&srv->d_primes, primes_need * sizeof(uint64_t)));
+                srv->primes_cap = primes_need;
+            }
+            if (class_need > srv->class_cap) {
+                cudaFree(srv->d_codes);
+                cudaFree(srv->d_items);
+                srv->d_codes = nullptr;
+                srv->d_items = nullptr;
+                srv->class_cap = 0;
+                CTX_TRY(cudaMalloc(&srv->d_codes, class_need * sizeof(uint32_t)));
+                CTX_TRY(cudaMalloc(&srv->d_items, class_need * sizeof(ClassItem)));
+                srv->class_cap = class_need;
+            }
+        }
+        int rc = sieve_prepare_base(ctx_workspace(ctx), maxhi, st, err);
+        if (!rc)
+            rc = sieve_prepare_windows(ctx_workspace(ctx), S, err);
+        if (rc)
+            return ctx_fail(ctx, rc, err);
+        // this tick's active lists (slot numbers), in its own staging region
+        const uint32_t region = (uint32_t)(srv->tick_count % ctd_server::TICKS_IN_FLIGHT) * srv->adm.max_active;
+        uint32_t *h_act = srv->h_active + region;
+        uint32_t *d_act = srv->d_active + region;
+        uint32_t used = 0;
+        for (auto &kv : byseg) {
+            const uint64_t slo = kv.first * S;
+            uint64_t lo = ~0ull, hi = 0;
+            bool any_cls = false;
+            const uint32_t first = used;
+            std::vector<uint32_t> ks = kv.second;
+            std::stable_sort(ks.begin(), ks.end(), [&](uint32_t x, uint32_t y) {
+                const ctd_job &a = srv->running[x].job, &c = srv->running[y].job;
+                return (double)(a.n1 - a.n0) * term_cost(a.family) > (double)(c.n1 - c.n0) * term_cost(c.family);
+            });
+            for (uint32_t k : ks) {
+                ctd_server::Job &j = srv->running[k];
+                lo = std::min(lo, j.cursor);
+                const uint64_t upto = std::min(j.job.f1, slo + S);
+                hi = std::max(hi, upto);
+                any_cls |= srv->h_stage[j.slot].classified != 0;
+                h_act[used++] = j.slot;
+                j.cursor = upto;  // the device cursor moves the same way
+            }
+            CTX_TRY(cudaMemcpyAsync(d_act + first, h_act + first, (used - first) * sizeof(uint32_t),
+                                    cudaMemcpyHostToDevice, st));
+            const uint64_t *d_count = nullptr;
+            rc = sieve_odd_async(ctx_workspace(ctx), lo, hi, srv->d_primes, srv->primes_cap, &d_count, st, err);
+            if (!rc) {
+                BatchScratch bs;
+                bs.spans = srv->d_spans;
+                bs.ctl = srv->d_ctl;
+                bs.codes = srv->d_codes;
+                bs.items = srv->d_items;
+                bs.bucket_count = srv->d_bucket;
+                bs.bucket_base = srv->d_bucket + 2ull * (used - first) * CLASS_BUCKETS;
+                rc = launch_batch(srv->d_jobs, d_act + first, used - first, any_cls, srv->d_primes, d_count, lo, hi,
+                                  bs, ctx_sm_count(ctx), st, err);
+            }
+            if (rc)
+                return ctx_fail(ctx, rc, err);
+        }
+        // jobs that reached the end of their range: results to the host
+        for (ctd_server::Job &j : srv->running) {
+            if (j.finishing || j.cursor < j.job.f1)
+                continue;
+            const uint64_t N = j.job.n1 - j.job.n0;
+            CTX_TRY(cudaMallocHost(&j.h_counts, N * sizeof(uint32_t)));
+            CTX_TRY(cudaMallocHost(&j.h_factors, N * j.job.max_factors * sizeof(uint64_t)));
+            CTX_TRY(cudaMemcpyAsync(j.h_counts, j.d_counts, N * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+            CTX_TRY(cudaMemcpyAsync(j.h_factors, j.d_factors, N * j.job.max_factors * sizeof(uint64_t),
+                                    cudaMemcpyDeviceToHost, st));
+            CTX_TRY(cudaFreeAsync(j.d_counts, st));
+            CTX_TRY(cudaFreeAsync(j.d_factors, st));
+            j.d_counts = nullptr;
+            j.d_factors = nullptr;
+            CTX_TRY(cudaEventCreateWithFlags(&j.done_event, cudaEventDisableTiming));
+            CTX_TRY(cudaEventRecord(j.done_event, st));
+            j.finishing = true;
+        }
+        cudaEvent_t ev;
+        CTX_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        CTX_TRY(cudaEventRecord(ev, st));
+        srv->inflight.push_back(ev);
+        ++srv->tick_count;
+    } else if (!srv->running.empty()) {
+        // nothing left to queue: wait for the oldest finishing job
+        for (ctd_server::Job &j : srv->running)
+            if (j.finishing) {
+                CTX_TRY(cudaEventSynchronize(j.done_event));
+                break;
+            }
+    }
     return CTD_OK;
 }
 
@@ -512,8 +824,11 @@ int ctd_serve_fetch(ctd_server *srv, uint64_t id, uint32_t *counts, uint64_t *fa
     auto it = srv->done.find(id);
     if (it == srv->done.end())
         return ctx_fail(srv->ctx, CTD_ERR_NOT_FOUND, "ctd_serve_fetch: job not finished or unknown");
-    std::memcpy(counts, it->second.first.data(), it->second.first.size() * sizeof(uint32_t));
-    std::memcpy(factors, it->second.second.data(), it->second.second.size() * sizeof(uint64_t));
+    ctd_server::Job &j = it->second;
+    const uint64_t N = j.job.n1 - j.job.n0;
+    std::memcpy(counts, j.h_counts, N * sizeof(uint32_t));
+    std::memcpy(factors, j.h_factors, N * j.job.max_factors * sizeof(uint64_t));
+    free_job_host(j);
     srv->done.erase(it);
     return CTD_OK;
 }

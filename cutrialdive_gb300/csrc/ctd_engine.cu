@@ -21,6 +21,7 @@ struct ctd_ctx {
     cudaStream_t stream = nullptr;
     SieveWorkspace *ws = nullptr;
     ResidueScratch *rs = nullptr;
+    BatchCache *batch = nullptr;
     std::string last_error;
     int grid_override = 0;
     int block_override = 0;
@@ -221,6 +222,13 @@ int ctx_device(const ctd_ctx *ctx) { return ctx->device; }
 int ctx_sm_count(const ctd_ctx *ctx) { return ctx->sm_count; }
 cudaStream_t ctx_stream(const ctd_ctx *ctx) { return ctx->stream; }
 SieveWorkspace *ctx_workspace(const ctd_ctx *ctx) { return ctx->ws; }
+BatchCache *&ctx_batch_cache(ctd_ctx *ctx) { return ctx->batch; }
+ctd_tuning ctx_tuning(ctd_ctx *ctx, uint32_t family)
+{
+    ctd_tuning t{};
+    ctd_get_tuning(ctx, family, &t);
+    return t;
+}
 int ctx_fail(ctd_ctx *ctx, int code, const std::string &msg) { return fail(ctx, code, msg); }
 }  // namespace ctd
 
@@ -304,6 +312,7 @@ void ctd_close(ctd_ctx *ctx)
         cudaStreamSynchronize(ctx->stream);
     sieve_workspace_destroy(ctx->ws);
     residue_scratch_destroy(ctx->rs);
+    batch_cache_destroy(ctx->batch);
     cudaFree(ctx->d_primes);
     cudaFree(ctx->d_counts);
     cudaFree(ctx->d_factors);

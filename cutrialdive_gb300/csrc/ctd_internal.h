@@ -103,8 +103,19 @@ int noalloc_prepare(int device, std::string &err);
 // long index ranges): per prime its power-residue class, then the primes
 // regrouped by class so a warp's lanes walk classes of equal length.  Owned
 // by a context; grown on demand (never during a graph capture).
-struct ClassCounters;
-struct ClassItem;
+// classes: the divisors of 2^3 * 3 * 5 * 7, ranked by size
+constexpr uint32_t CLASS_BUCKETS = 32;
+struct ClassCounters {
+    uint32_t count[CLASS_BUCKETS];  // primes per class
+    uint32_t fill[CLASS_BUCKETS];   // regroup cursors
+    unsigned long long next;        // walk work counter
+};
+// a prime with its class code (M << 16 | r)
+struct ClassItem {
+    uint64_t p;
+    uint32_t code;
+    uint32_t pad;
+};
 struct ResidueScratch {
     int device = 0;
     int sm_count = 1;
@@ -126,26 +137,53 @@ int prepare_residue_tables(int device, std::string &err);
 // long ranges go through the classified launches (classify, regroup, walk).
 int launch_residues(const JobView &view, const uint64_t *d_primes, uint64_t nprimes, int grid, int block,
                     cudaStream_t stream, std::string &err, ResidueScratch *scratch = nullptr);
-// One job of a batched launch: its view (factors buffer, index range) and
-// its prime range [f0, f1).
+// One job of a batched launch: its view (factors buffer, index range,
+// tiles), its odd-prime range [f0, f1) and whether it walks power-residue
+// classes (doubling families over long ranges).
+// `cursor` is the job's progress on the device: primes below it are done;
+// each segment's bounds kernel starts the job at max(f0, cursor) and moves
+// the cursor to the segment's end.
 struct BatchJob {
     JobView view;
     uint64_t f0, f1;
+    uint64_t cursor;
+    uint32_t classified;
+    uint32_t pad;
 };
-// Per active job of a batched launch: first prime index of its sub-range,
-// item count, exclusive item prefix (entry nactive holds the total).
+// Per active job of a batched segment: its primes [pbeg, pend) in the
+// segment's list, its offset in the class buffers, its (prime, tile) units
+// and the exclusive prefix of warp items (entry nactive holds the totals).
 struct BatchSpan {
-    uint64_t pbeg;
-    uint64_t items;
-    uint64_t prefix;
+    uint64_t pbeg, pend;
+    uint64_t coff;
+    uint64_t units;
+    uint64_t warp_prefix;
 };
-// Bounds kernel + one batched residue kernel over the active jobs (all of
-// `family`) for the primes of [lo, hi) in d_primes; the prime count is read
-// from *d_count on the device.  d_spans holds nactive + 1 entries.
-int launch_batch(uint32_t family, const BatchJob *d_jobs, const uint32_t *d_active, uint32_t nactive,
-                 const uint64_t *d_primes, const uint64_t *d_count, uint64_t lo, uint64_t hi, BatchSpan *d_spans,
-                 int grid, cudaStream_t stream, std::string &err);
-int batch_blocks_per_sm(uint32_t family);
+struct BatchControl {
+    uint64_t nclass;          // (classified job, prime) pairs
+    uint64_t total_warps;     // warp items of the walk
+    unsigned long long next;  // walk work counter
+};
+// Device scratch of one batched segment (sized by the caller):
+// spans[nactive + 1], codes/items[class pairs], bucket_count[2 * nactive *
+// CLASS_BUCKETS] (counts, then regroup cursors), bucket_base[nactive *
+// CLASS_BUCKETS].
+struct BatchScratch {
+    BatchSpan *spans;
+    BatchControl *ctl;
+    uint32_t *codes;
+    ClassItem *items;
+    uint32_t *bucket_count;
+    uint32_t *bucket_base;
+};
+// The kernels of one batched segment over the primes of [lo, hi) in
+// d_primes (count read from *d_count on the device): bounds, classes (when
+// any active job is classified), plan, regroup and one walk launch for all
+// families.  Nothing waits on the host.  Each active job's device cursor
+// moves to the end of its part of [lo, hi).
+int launch_batch(BatchJob *d_jobs, const uint32_t *d_active, uint32_t nactive, bool any_classified,
+                 const uint64_t *d_primes, const uint64_t *d_count, uint64_t lo, uint64_t hi,
+                 const BatchScratch &bs, int sm_count, cudaStream_t stream, std::string &err);
 // Odd primes of [lo, hi) into d_out without waiting on the host; the count
 // is left at *count_out (device memory, owned by the workspace).  Base primes
 // must already cover sqrt(hi) (sieve_prepare_base).
@@ -153,6 +191,10 @@ int sieve_prepare_base(SieveWorkspace *ws, uint64_t hi, cudaStream_t stream, std
 int sieve_prepare_windows(SieveWorkspace *ws, uint64_t max_width, std::string &err);
 int sieve_odd_async(SieveWorkspace *ws, uint64_t lo, uint64_t hi, uint64_t *d_out, uint64_t capacity,
                     const uint64_t **count_out, cudaStream_t stream, std::string &err);
+// Changes whenever sieve_odd_async's launches would take other arguments
+// for the same range (base primes extended, scratch regrown): part of the
+// key under which a captured schedule may be replayed.
+uint64_t sieve_state_key(const SieveWorkspace *ws);
 
 // Resident CTAs per SM of the family's residue kernel at `block` threads
 // (0 if the query fails); the persistent grid is SMs x this.
@@ -163,11 +205,19 @@ int launch_mod2(const JobView &view, cudaStream_t stream, std::string &err);
 uint64_t kernel_launch_count();
 void note_kernel_launch();
 
+// Device buffers and the captured schedule of ctd_batch_run, kept by a
+// context across calls (ctd_batch.cu).
+struct BatchCache;
+void batch_cache_destroy(BatchCache *bc);
+
 // Context accessors for entry points defined outside ctd_engine.cu.
 int ctx_device(const ctd_ctx *ctx);
 int ctx_sm_count(const ctd_ctx *ctx);
 cudaStream_t ctx_stream(const ctd_ctx *ctx);
 SieveWorkspace *ctx_workspace(const ctd_ctx *ctx);
+BatchCache *&ctx_batch_cache(ctd_ctx *ctx);
+// the launch/tiling parameters in force for a family (defaults when untuned)
+ctd_tuning ctx_tuning(ctd_ctx *ctx, uint32_t family);
 int ctx_fail(ctd_ctx *ctx, int code, const std::string &msg);
 
 }  // namespace ctd

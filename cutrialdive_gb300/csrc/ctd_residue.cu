@@ -579,7 +579,7 @@ __device__ __forceinline__ void run_doubling(const JobView &job, uint64_t p, uin
 // ------------------------------------- doubling over power-residue classes
 // For long index ranges the doubling families first classify each prime
 // (ctd_powres.cuh): every zero n of k*2^n-+1 (2^n-1) mod p satisfies
-// n = r (mod M) for a class M | 2^6 * 3 * 5 * 7 read off the 2-power, 3rd,
+// n = r (mod M) for a class M | 2^3 * 3 * 5 * 7 read off the 2-power, 3rd,
 // 5th and 7th power residues of 2 and of the target, and about 40 % of the
 // primes (Proth k = 3) divide no term at all.  The walk then visits only
 // n = r, r + M, r + 2M, ... with the same baby-step/giant-step blocks over
@@ -614,12 +614,12 @@ __device__ __forceinline__ uint32_t doubling_class_code(const JobView &job, uint
 {
     if (p >= (1ull << 63))
         return 1u << 16;
-    const uint64_t wt = doubling_target<FAM>(job, p);
-    if (!wt)
-        return 0;
+    const uint64_t k = FAM == MERSENNE ? 1 : (job.param < p ? job.param : job.param % p);
+    if (!k)
+        return 0;  // p | k: k 2^n -+ 1 = -+1 (mod p), never zero
     Mont m;
     m.init(p);
-    const PowerClass c = doubling_class(m, m.to(wt));
+    const PowerClass c = doubling_class(m, k, FAM == PROTH);
     return c.M ? (c.M << 16) | c.r : 0u;
 }
 
@@ -638,7 +638,14 @@ __device__ void run_doubling_class(const JobView &job, uint64_t p, uint32_t M, u
     const uint64_t wt = doubling_target<FAM>(job, p);
     const uint64_t nr = nf < p - 1 ? nf : nf % (p - 1);
     uint64_t w = m.from(m.pow2(p - 1 - nr));  // 2^-nf (Fermat)
-    const uint64_t HM = small_pow(m, m.to((p + 1) >> 1), M);  // 2^-M, Montgomery form
+    // 2^-M in Montgomery form: left-to-right powering of 2^-1, each set bit a
+    // halving of the Montgomery representative ((x R) / 2 = (x / 2) R)
+    uint64_t HM = m.one;
+    for (int b = 31 - __clz(M); b >= 0; --b) {
+        HM = m.mul(HM, HM);
+        if ((M >> b) & 1)
+            HM = half63(HM, p);
+    }
     const uint64_t g = m.from(HM);
     const MulConst step{g, m.shoup(g)};  // w -> w 2^-M: the next term of the class
     const uint64_t at0 = nf - job.n0;
@@ -1518,21 +1525,7 @@ residue_kernel(JobView job, const uint64_t *__restrict__ primes, uint64_t nprime
 //                    walk classes of the same M -- equal lengths, no lane
 //                    waiting on a longer one.
 // The classes are the divisors of 2^6 * 105 (56 of them), ranked by size.
-constexpr uint32_t CLASS_BUCKETS = 56;
-
-struct ClassCounters {
-    uint32_t count[CLASS_BUCKETS];  // primes per class
-    uint32_t fill[CLASS_BUCKETS];   // regroup cursors
-    unsigned long long next;        // walk work counter
-};
-
-struct ClassItem {
-    uint64_t p;
-    uint32_t code;
-    uint32_t pad;
-};
-
-// rank of M among the divisors of 2^6 * 3 * 5 * 7
+// rank of M among the divisors of 2^3 * 3 * 5 * 7
 __device__ __forceinline__ uint32_t class_bucket(uint32_t M)
 {
     uint32_t rank = 0;
@@ -1622,94 +1615,6 @@ class_walk_kernel(JobView job, const ClassItem *__restrict__ items, ClassCounter
     }
 }
 
-// ------------------------------------------------------ batched launches
-// Several jobs over one segment's prime list.  A bounds kernel finds each
-// active job's sub-range of the (sorted) primes and the exclusive prefix of
-// their item counts, reading the prime count from device memory so nothing
-// waits on the host; then one launch per family walks every (job, prime)
-// item.  Used by the batched and served engines (ctd_batch.cu).
-
-__device__ __forceinline__ uint64_t lower_bound_u64(const uint64_t *a, uint64_t n, uint64_t x)
-{
-    uint64_t lo = 0, hi = n;
-    while (lo < hi) {
-        uint64_t mid = (lo + hi) >> 1;
-        if (a[mid] < x)
-            lo = mid + 1;
-        else
-            hi = mid;
-    }
-    return lo;
-}
-
-__global__ void __launch_bounds__(1024) batch_bounds_kernel(const BatchJob *__restrict__ jobs,
-                                                            const uint32_t *__restrict__ active, uint32_t nactive,
-                                                            const uint64_t *__restrict__ primes,
-                                                            const uint64_t *__restrict__ d_count, uint64_t lo,
-                                                            uint64_t hi, BatchSpan *__restrict__ spans)
-{
-    const uint64_t n = *d_count;
-    for (uint32_t i = threadIdx.x; i < nactive; i += blockDim.x) {
-        const BatchJob &j = jobs[active[i]];
-        const uint64_t a = j.f0 > lo ? j.f0 : lo;
-        const uint64_t b = j.f1 < hi ? j.f1 : hi;
-        uint64_t pb = 0, pe = 0;
-        if (a < b) {
-            pb = lower_bound_u64(primes, n, a);
-            pe = lower_bound_u64(primes, n, b);
-        }
-        spans[i].pbeg = pb;
-        spans[i].items = pe - pb;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint64_t run = 0;
-        for (uint32_t i = 0; i < nactive; ++i) {
-            spans[i].prefix = run;
-            run += spans[i].items;
-        }
-        spans[nactive].prefix = run;  // total items
-        spans[nactive].items = 0;     // the batch kernel's work counter
-    }
-}
-
-// Persistent grid over a device work queue: each warp takes the next 32
-// items (one prime of one job each) from a counter the bounds kernel reset;
-// the host orders a launch's jobs longest index range first, so the long
-// items start early and the short ones fill in at the end.
-template <uint32_t FAM>
-__global__ void __launch_bounds__(256, min_ctas_per_sm(FAM))
-batch_kernel(const BatchJob *__restrict__ jobs, const uint32_t *__restrict__ active, uint32_t nactive,
-             const uint64_t *__restrict__ primes, BatchSpan *__restrict__ spans)
-{
-    const uint64_t total = spans[nactive].prefix;
-    unsigned long long *next = reinterpret_cast<unsigned long long *>(&spans[nactive].items);
-    const uint32_t lane = threadIdx.x & 31u;
-    for (;;) {
-        unsigned long long base = 0;
-        if (lane == 0)
-            base = atomicAdd(next, 32ull);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= total)
-            break;
-        const uint64_t k = base + lane;
-        if (k < total) {
-            // the active job holding item k: last prefix <= k
-            uint32_t lo = 0, hi = nactive;
-            while (hi - lo > 1) {
-                uint32_t mid = (lo + hi) >> 1;
-                if (spans[mid].prefix <= k)
-                    lo = mid;
-                else
-                    hi = mid;
-            }
-            const JobView &v = jobs[active[lo]].view;
-            const uint64_t p = primes[spans[lo].pbeg + (k - spans[lo].prefix)];
-            run_item<FAM>(v, p, v.n0, v.n1);
-        }
-    }
-}
-
 // dynamic shared memory of a family's kernels at `block` threads
 template <uint32_t FAM>
 constexpr size_t smem_bytes(int block)
@@ -1726,84 +1631,291 @@ static cudaError_t allow_smem(K kernel, size_t bytes)
     return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-template <uint32_t FAM>
-static cudaError_t launch_batch_fam(const BatchJob *jobs, const uint32_t *active, uint32_t nactive,
-                                    const uint64_t *primes, BatchSpan *spans, int grid, cudaStream_t st)
+// ------------------------------------------------------ batched launches
+// Many jobs over one segment's prime list, any mix of families, in one
+// persistent walk launch.  Per segment (all on the stream, nothing waits on
+// the host, so a whole schedule is captured in one CUDA graph):
+//   batch_bounds_kernel   each active job's sub-range of the sorted primes,
+//                         and for the classified (doubling) jobs their
+//                         offsets in the class buffers;
+//   batch_classify_kernel power-residue class of every (classified job,
+//                         prime) pair, counted per job and class;
+//   batch_plan_kernel     per job: class bases, its (prime, tile) units and
+//                         the exclusive prefix of warp items over the jobs;
+//   batch_regroup_kernel  the classified pairs written class by class;
+//   batch_walk_kernel     a persistent grid taking one warp item (32 units
+//                         of one job: same family, same class) at a time
+//                         from a counter -- every family in one kernel.
+// Work items are (job, 32 primes, index tile): long index ranges are cut
+// into tiles that start with the families' O(log n) jumps, so a long job is
+// spread over many warps instead of serialising on its primes.
+
+__device__ __forceinline__ uint64_t lower_bound_u64(const uint64_t *a, uint64_t n, uint64_t x)
 {
-    const size_t sm = smem_bytes<FAM>(256);
-    cudaError_t e = allow_smem(batch_kernel<FAM>, sm);
-    if (e != cudaSuccess)
-        return e;
-    batch_kernel<FAM><<<grid, 256, sm, st>>>(jobs, active, nactive, primes, spans);
-    return cudaGetLastError();
+    uint64_t lo = 0, hi = n;
+    while (lo < hi) {
+        uint64_t mid = (lo + hi) >> 1;
+        if (a[mid] < x)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
 }
 
-int launch_batch(uint32_t family, const BatchJob *d_jobs, const uint32_t *d_active, uint32_t nactive,
-                 const uint64_t *d_primes, const uint64_t *d_count, uint64_t lo, uint64_t hi, BatchSpan *d_spans,
-                 int grid, cudaStream_t st, std::string &err)
+// the last active job i with key(i) <= x (keys nondecreasing, key(0) <= x)
+template <class Key>
+__device__ __forceinline__ uint32_t last_le(uint32_t n, uint64_t x, Key key)
+{
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (key(mid) <= x)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(1024) batch_bounds_kernel(BatchJob *__restrict__ jobs,
+                                                            const uint32_t *__restrict__ active, uint32_t nactive,
+                                                            const uint64_t *__restrict__ primes,
+                                                            const uint64_t *__restrict__ d_count, uint64_t lo,
+                                                            uint64_t hi, BatchSpan *__restrict__ spans,
+                                                            BatchControl *__restrict__ ctl)
+{
+    const uint64_t n = *d_count;
+    for (uint32_t i = threadIdx.x; i < nactive; i += blockDim.x) {
+        BatchJob &j = jobs[active[i]];
+        // the job's primes of this segment not yet done: [max(f0, cursor, lo), min(f1, hi))
+        uint64_t a = j.f0 > lo ? j.f0 : lo;
+        a = j.cursor > a ? j.cursor : a;
+        const uint64_t b = j.f1 < hi ? j.f1 : hi;
+        uint64_t pb = 0, pe = 0;
+        if (a < b) {
+            pb = lower_bound_u64(primes, n, a);
+            pe = lower_bound_u64(primes, n, b);
+            j.cursor = b;  // the walk of this segment completes them
+        }
+        spans[i].pbeg = pb;
+        spans[i].pend = pe;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint64_t run = 0;
+        for (uint32_t i = 0; i < nactive; ++i) {
+            spans[i].coff = run;
+            if (jobs[active[i]].classified)
+                run += spans[i].pend - spans[i].pbeg;
+        }
+        spans[nactive].coff = run;
+        ctl->nclass = run;
+        ctl->next = 0;
+    }
+}
+
+// the classified job holding class pair t
+__device__ __forceinline__ uint32_t class_job(const BatchSpan *spans, uint32_t nactive, uint64_t t)
+{
+    return last_le(nactive, t, [&](uint32_t i) { return spans[i].coff; });
+}
+
+__global__ void __launch_bounds__(256) batch_classify_kernel(const BatchJob *__restrict__ jobs,
+                                                             const uint32_t *__restrict__ active, uint32_t nactive,
+                                                             const uint64_t *__restrict__ primes,
+                                                             const BatchSpan *__restrict__ spans,
+                                                             const BatchControl *__restrict__ ctl,
+                                                             uint32_t *__restrict__ codes,
+                                                             uint32_t *__restrict__ bucket_count)
+{
+    const uint64_t total = ctl->nclass;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
+        const uint32_t i = class_job(spans, nactive, t);
+        const JobView &v = jobs[active[i]].view;
+        const uint64_t p = primes[spans[i].pbeg + (t - spans[i].coff)];
+        const uint32_t code = v.family == PROTH    ? doubling_class_code<PROTH>(v, p)
+                              : v.family == RIESEL ? doubling_class_code<RIESEL>(v, p)
+                                                   : doubling_class_code<MERSENNE>(v, p);
+        codes[t] = code;
+        if (code)
+            aggregated_increment(bucket_count, i * CLASS_BUCKETS + class_bucket(code >> 16));
+    }
+}
+
+__global__ void __launch_bounds__(1024) batch_plan_kernel(const BatchJob *__restrict__ jobs,
+                                                          const uint32_t *__restrict__ active, uint32_t nactive,
+                                                          BatchSpan *__restrict__ spans, BatchControl *__restrict__ ctl,
+                                                          const uint32_t *__restrict__ bucket_count,
+                                                          uint32_t *__restrict__ bucket_base)
+{
+    for (uint32_t i = threadIdx.x; i < nactive; i += blockDim.x) {
+        const BatchJob &j = jobs[active[i]];
+        uint64_t primes_i = spans[i].pend - spans[i].pbeg;
+        if (j.classified) {
+            uint64_t run = 0;
+            for (uint32_t b = 0; b < CLASS_BUCKETS; ++b) {
+                bucket_base[i * CLASS_BUCKETS + b] = (uint32_t)run;
+                run += bucket_count[i * CLASS_BUCKETS + b];
+            }
+            primes_i = run;  // pairs with a class (the others divide no term)
+        }
+        spans[i].units = primes_i * j.view.tiles;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint64_t run = 0;
+        for (uint32_t i = 0; i < nactive; ++i) {
+            spans[i].warp_prefix = run;
+            run += (spans[i].units + 31) / 32;
+        }
+        spans[nactive].warp_prefix = run;
+        ctl->total_warps = run;
+    }
+}
+
+__global__ void __launch_bounds__(256) batch_regroup_kernel(const uint32_t *__restrict__ active, uint32_t nactive,
+                                                            const uint64_t *__restrict__ primes,
+                                                            const BatchSpan *__restrict__ spans,
+                                                            const BatchControl *__restrict__ ctl,
+                                                            const uint32_t *__restrict__ codes,
+                                                            const uint32_t *__restrict__ bucket_base,
+                                                            uint32_t *__restrict__ bucket_fill,
+                                                            ClassItem *__restrict__ items)
+{
+    const uint64_t total = ctl->nclass;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
+        const uint32_t code = codes[t];
+        if (!code)
+            continue;
+        const uint32_t i = class_job(spans, nactive, t);
+        const uint32_t key = i * CLASS_BUCKETS + class_bucket(code >> 16);
+        const uint64_t pos = spans[i].coff + bucket_base[key] + aggregated_increment(bucket_fill, key);
+        items[pos] = ClassItem{primes[spans[i].pbeg + (t - spans[i].coff)], code, 0};
+    }
+}
+
+// one (prime, tile) unit of a job of any family
+__device__ __forceinline__ void batch_unit(const BatchJob &j, uint64_t p, uint32_t code, uint64_t s, uint64_t e)
+{
+    const JobView &v = j.view;
+    if (j.classified && p < (1ull << 63)) {
+        switch (v.family) {
+        case PROTH: run_doubling_class<PROTH>(v, p, code >> 16, code & 0xffffu, s, e); return;
+        case RIESEL: run_doubling_class<RIESEL>(v, p, code >> 16, code & 0xffffu, s, e); return;
+        default: run_doubling_class<MERSENNE>(v, p, code >> 16, code & 0xffffu, s, e); return;
+        }
+    }
+    switch (v.family) {
+    case MERSENNE: run_item<MERSENNE>(v, p, s, e); break;
+    case PROTH: run_item<PROTH>(v, p, s, e); break;
+    case RIESEL: run_item<RIESEL>(v, p, s, e); break;
+    case SMARANDACHE: run_item<SMARANDACHE>(v, p, s, e); break;
+    case FIBONACCI: run_item<FIBONACCI>(v, p, s, e); break;
+    case LUCAS: run_item<LUCAS>(v, p, s, e); break;
+    case PROTH_FIXED_N: run_item<PROTH_FIXED_N>(v, p, s, e); break;
+    case RIESEL_FIXED_N: run_item<RIESEL_FIXED_N>(v, p, s, e); break;
+    case TRIBONACCI: run_item<TRIBONACCI>(v, p, s, e); break;
+    default: run_item<PEANO>(v, p, s, e); break;
+    }
+}
+
+constexpr int BATCH_CTAS_PER_SM = 3;  // the target filter's 64 KiB per CTA and 80 registers a thread
+
+__global__ void __launch_bounds__(256, BATCH_CTAS_PER_SM)
+batch_walk_kernel(const BatchJob *__restrict__ jobs, const uint32_t *__restrict__ active, uint32_t nactive,
+                  const uint64_t *__restrict__ primes, const BatchSpan *__restrict__ spans,
+                  BatchControl *__restrict__ ctl, const ClassItem *__restrict__ items)
+{
+    const uint64_t total = ctl->total_warps;
+    const uint32_t lane = threadIdx.x & 31u;
+    for (;;) {
+        unsigned long long w = 0;
+        if (lane == 0)
+            w = atomicAdd(&ctl->next, 1ull);
+        w = __shfl_sync(0xffffffffu, w, 0);
+        if (w >= total)
+            break;
+        const uint32_t i = last_le(nactive, w, [&](uint32_t k) { return spans[k].warp_prefix; });
+        const uint64_t u = (w - spans[i].warp_prefix) * 32 + lane;
+        if (u < spans[i].units) {
+            const BatchJob &j = jobs[active[i]];
+            const uint32_t tiles = j.view.tiles;
+            const uint64_t idx = tiles == 1 ? u : u / tiles;
+            const uint64_t t = u - idx * tiles;
+            const uint64_t s = j.view.n0 + t * j.view.tile_len;
+            const uint64_t e = s + j.view.tile_len < j.view.n1 ? s + j.view.tile_len : j.view.n1;
+            uint64_t p;
+            uint32_t code = 0;
+            if (j.classified) {
+                const ClassItem it = items[spans[i].coff + idx];
+                p = it.p;
+                code = it.code;
+            } else {
+                p = primes[spans[i].pbeg + idx];
+            }
+            if (s < e)
+                batch_unit(j, p, code, s, e);
+        }
+    }
+}
+
+int launch_batch(BatchJob *d_jobs, const uint32_t *d_active, uint32_t nactive, bool any_classified,
+                 const uint64_t *d_primes, const uint64_t *d_count, uint64_t lo, uint64_t hi,
+                 const BatchScratch &bs, int sm_count, cudaStream_t st, std::string &err)
 {
     if (!nactive)
         return CTD_OK;
-    batch_bounds_kernel<<<1, 1024, 0, st>>>(d_jobs, d_active, nactive, d_primes, d_count, lo, hi, d_spans);
-    cudaError_t rc = cudaGetLastError();
+    cudaError_t rc = cudaSuccess;
+    const int cgrid = sm_count * 8;
+    if (any_classified)
+        rc = cudaMemsetAsync(bs.bucket_count, 0, 2ull * nactive * CLASS_BUCKETS * sizeof(uint32_t), st);
     if (rc == cudaSuccess) {
+        batch_bounds_kernel<<<1, 1024, 0, st>>>(d_jobs, d_active, nactive, d_primes, d_count, lo, hi, bs.spans,
+                                                bs.ctl);
+        rc = cudaGetLastError();
         note_kernel_launch();
-        switch (family) {
-        case MERSENNE: rc = launch_batch_fam<MERSENNE>(d_jobs, d_active, nactive, d_primes, d_spans, grid, st); break;
-        case PROTH: rc = launch_batch_fam<PROTH>(d_jobs, d_active, nactive, d_primes, d_spans, grid, st); break;
-        case RIESEL: rc = launch_batch_fam<RIESEL>(d_jobs, d_active, nactive, d_primes, d_spans, grid, st); break;
-        case SMARANDACHE:
-            rc = launch_batch_fam<SMARANDACHE>(d_jobs, d_active, nactive, d_primes, d_spans, grid, st);
-            break;
-        case FIBONACCI: rc = launch_batch_fam<FIBONACCI>(d_jobs, d_active, nactive, d_primes, d_spans, grid, st); break;
-        case LUCAS: rc = launch_batch_fam<LUCAS>(d_jobs, d_active, nactive, d_primes, d_spans, grid, st); break;
-        case PROTH_FIXED_N:
-            rc = launch_batch_fam<PROTH_FIXED_N>(d_jobs, d_active, nactive, d_primes, d_spans, grid, st);
-            break;
-        case RIESEL_FIXED_N:
-            rc = launch_batch_fam<RIESEL_FIXED_N>(d_jobs, d_active, nactive, d_primes, d_spans, grid, st);
-            break;
-        case TRIBONACCI:
-            rc = launch_batch_fam<TRIBONACCI>(d_jobs, d_active, nactive, d_primes, d_spans, grid, st);
-            break;
-        case PEANO: rc = launch_batch_fam<PEANO>(d_jobs, d_active, nactive, d_primes, d_spans, grid, st); break;
-        default: err = "unknown sequence family"; return CTD_ERR_INVALID_ARGUMENT;
+    }
+    if (rc == cudaSuccess && any_classified) {
+        batch_classify_kernel<<<cgrid, 256, 0, st>>>(d_jobs, d_active, nactive, d_primes, bs.spans, bs.ctl,
+                                                     bs.codes, bs.bucket_count);
+        rc = cudaGetLastError();
+        note_kernel_launch();
+    }
+    if (rc == cudaSuccess) {
+        batch_plan_kernel<<<1, 1024, 0, st>>>(d_jobs, d_active, nactive, bs.spans, bs.ctl, bs.bucket_count,
+                                              bs.bucket_base);
+        rc = cudaGetLastError();
+        note_kernel_launch();
+    }
+    if (rc == cudaSuccess && any_classified) {
+        // bucket_fill follows bucket_count (cleared together above)
+        batch_regroup_kernel<<<cgrid, 256, 0, st>>>(d_active, nactive, d_primes, bs.spans, bs.ctl, bs.codes,
+                                                    bs.bucket_base, bs.bucket_count + nactive * CLASS_BUCKETS,
+                                                    bs.items);
+        rc = cudaGetLastError();
+        note_kernel_launch();
+    }
+    if (rc == cudaSuccess) {
+        const size_t sm = (size_t)FILTER_WORDS * sizeof(uint32_t) * 256;
+        rc = allow_smem(batch_walk_kernel, sm);
+        int occ = 0;
+        if (rc == cudaSuccess)
+            rc = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_walk_kernel, 256, sm);
+        if (rc == cudaSuccess) {
+            batch_walk_kernel<<<sm_count * (occ > 0 ? occ : 1), 256, sm, st>>>(d_jobs, d_active, nactive, d_primes,
+                                                                              bs.spans, bs.ctl, bs.items);
+            rc = cudaGetLastError();
+            note_kernel_launch();
         }
     }
     if (rc != cudaSuccess) {
         err = std::string("batched residue launch: ") + cudaGetErrorString(rc);
         return CTD_ERR_CUDA;
     }
-    note_kernel_launch();
     return CTD_OK;
-}
-
-template <uint32_t FAM>
-static int batch_occupancy(int block)
-{
-    int n = 0;
-    const size_t sm = smem_bytes<FAM>(block);
-    if (allow_smem(batch_kernel<FAM>, sm) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<FAM>, block, sm) != cudaSuccess)
-        return 0;
-    return n;
-}
-
-int batch_blocks_per_sm(uint32_t family)
-{
-    switch (family) {
-    case MERSENNE: return batch_occupancy<MERSENNE>(256);
-    case PROTH: return batch_occupancy<PROTH>(256);
-    case RIESEL: return batch_occupancy<RIESEL>(256);
-    case SMARANDACHE: return batch_occupancy<SMARANDACHE>(256);
-    case FIBONACCI: return batch_occupancy<FIBONACCI>(256);
-    case LUCAS: return batch_occupancy<LUCAS>(256);
-    case PROTH_FIXED_N: return batch_occupancy<PROTH_FIXED_N>(256);
-    case RIESEL_FIXED_N: return batch_occupancy<RIESEL_FIXED_N>(256);
-    case TRIBONACCI: return batch_occupancy<TRIBONACCI>(256);
-    case PEANO: return batch_occupancy<PEANO>(256);
-    default: return 0;
-    }
 }
 
 // --------------------------------------------------------- the prime 2

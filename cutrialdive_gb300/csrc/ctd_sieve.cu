@@ -482,6 +482,21 @@ int sieve_prepare_windows(SieveWorkspace *ws, uint64_t max_width, std::string &e
     return CTD_OK;
 }
 
+uint64_t sieve_state_key(const SieveWorkspace *ws)
+{
+    // FNV-1a over what sieve_odd_async's launches take besides the range
+    const uint64_t parts[] = {(uint64_t)(uintptr_t)ws->d_base, ws->nbase, (uint64_t)(uintptr_t)ws->d_bits,
+                              (uint64_t)(uintptr_t)ws->d_wcount, (uint64_t)(uintptr_t)ws->d_offsets,
+                              (uint64_t)ws->sm_count};
+    uint64_t h = 1469598103934665603ull;
+    for (uint64_t x : parts)
+        for (int b = 0; b < 8; ++b) {
+            h ^= (x >> (8 * b)) & 0xff;
+            h *= 1099511628211ull;
+        }
+    return h;
+}
+
 int sieve_odd_async(SieveWorkspace *ws, uint64_t lo, uint64_t hi, uint64_t *d_out, uint64_t capacity,
                     const uint64_t **count_out, cudaStream_t st, std::string &err)
 {

@@ -201,19 +201,28 @@ int ctd_mod2_device(ctd_ctx *ctx, const ctd_job *job, uint32_t *d_counts, uint64
 
 /* Runs `njobs` jobs together: the union of their prime ranges is walked in
  * aligned segments of `segment_length` (0 = 2^30); each segment is sieved
- * once on the device and consumed by every job covering it with one batched
- * residue launch per family.  With use_graph != 0 the whole schedule is
- * captured into one CUDA graph and launched once.  counts_inout[i] /
- * factors_inout[i] are job i's host factors buffers (resume state in,
- * results out). */
+ * once on the device and consumed by every job covering it in one
+ * persistent walk launch over (job, 32 primes, index tile) work items of
+ * all families.  With use_graph != 0 the whole schedule is captured into a
+ * CUDA graph and launched once; the context keeps the instantiated graph
+ * and its device buffers, so a later call with the same schedule replays it
+ * and one with the same shape updates it in place (ctd_batch_graph_stats
+ * counts each).  counts_inout[i] / factors_inout[i] are job i's host
+ * factors buffers (resume state in, results out). */
 int ctd_batch_run(ctd_ctx *ctx, const ctd_job *jobs, uint32_t njobs, uint32_t *const *counts_inout,
                   uint64_t *const *factors_inout, uint64_t segment_length, int use_graph);
+/* Graphs instantiated, updated in place and replayed by ctd_batch_run on this context. */
+int ctd_batch_graph_stats(ctd_ctx *ctx, uint64_t *instantiations, uint64_t *updates, uint64_t *replays);
 
 /* Continuous-batching server.  Submitted jobs queue; each ctd_serve_tick
- * admits queued jobs (arrival order) while fewer than max_active run and
- * their device buffers fit memory_budget, then advances every active job
- * over its next aligned prime segment in shared batched launches, and
- * reports the jobs that finished; ctd_serve_fetch returns (and releases) a
+ * collects the jobs whose results have arrived on the host, admits queued
+ * jobs (arrival order) while fewer than max_active run and their device
+ * buffers fit memory_budget (a job larger than the budget runs alone), and
+ * queues one more tick of work without waiting for the previous ticks (at
+ * most two ahead of the GPU): every running job advances over its next
+ * aligned prime segment, jobs in the same segment sharing its sieve and one
+ * walk launch.  Progress cursors live in the server's device job table and
+ * are moved by the kernels.  ctd_serve_fetch returns (and releases) a
  * finished job's factors buffer. */
 typedef struct ctd_server ctd_server;
 int ctd_serve_open(ctd_ctx *ctx, uint64_t memory_budget, uint32_t max_active, uint64_t segment_length,

@@ -13,7 +13,8 @@ int main()
     while (std::scanf("%llu %llu", &p, &wt) == 2) {
         ctd::Mont m;
         m.init(p);
-        const ctd::PowerClass c = ctd::doubling_class(m, m.to(wt));
+        // wt as -k with k = p - wt (the Proth form); the test covers every wt
+        const ctd::PowerClass c = ctd::doubling_class(m, p - wt, true);
         std::printf("%u %u\n", c.M, c.r);
     }
     return 0;

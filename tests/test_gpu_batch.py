@@ -120,3 +120,26 @@ def test_batch_rejects_invalid_jobs(eng):
     jobs[1] = ctd.CtdJob(O.PROTH, M, 0, 1, 10, 3, 100)  # k = 0 is rejected, as by the reference
     with pytest.raises(ctd.CtdError):
         eng.batch_run(jobs, bufs)
+
+
+def test_batch_graph_replayed_and_updated(eng):
+    """A second call with the same schedule replays the captured graph; one
+    with the same shape but other jobs updates it in place; both give the
+    oracle's results."""
+    before = eng.batch_graph_stats()
+    for _ in range(2):
+        jobs, bufs = new_buffers(MIX)
+        eng.batch_run(jobs, bufs, segment_length=W, use_graph=True)
+        for case, buf in zip(MIX, bufs):
+            assert_same(buf, case)
+    mid = eng.batch_graph_stats()
+    assert mid["replays"] >= before["replays"] + 1
+    # same shape (segments, active lists, launches), other launch arguments:
+    # the Smarandache job that includes the prime 2 ends one term earlier
+    other = [(f, p, n0, n1 - 1 if (f, p) == (O.SMARANDACHE, 10) else n1, f0, f1) for f, p, n0, n1, f0, f1 in MIX]
+    jobs, bufs = new_buffers(other)
+    eng.batch_run(jobs, bufs, segment_length=W, use_graph=True)
+    for case, buf in zip(other, bufs):
+        assert_same(buf, case)
+    after = eng.batch_graph_stats()
+    assert after["updates"] == mid["updates"] + 1 and after["instantiations"] == mid["instantiations"]
