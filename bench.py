@@ -1,19 +1,23 @@
 #!/usr/bin/env python3
 """Benchmark of the trial-factoring hot path on GB300.
 
-Default workload (the metric's plain single-job configuration): Proth k=3,
+Default line (the metric's plain single-job configuration): Proth k=3,
 S(n) = 3*2^n + 1 for n = 1..100000, trial-factored by every prime in
 [2^32, 2^34) produced by the device sieve.  One step = one 2^30-wide prime
-segment: device sieve -> primes in HBM -> residue kernel; the default 12
+segment: device sieve -> primes in HBM -> residue launches; the default 12
 steps cover the range once.  Unit of work: one (n, p) residue update;
-value = updates / s.
+value = updates / s.  The same line carries two more measurements of the
+metric ("batched vs plain; p50/p99 job latency"):
+  * "batched": the 64-job mix (seed 1234), each job's TF range cut to its
+    first 1/64, through one ctd_batch_run against the same jobs one by one
+    through ctd_run_plain, both on 2^30 segments; outputs checked against
+    each other and against the reference engine's factor files;
+  * "served": Poisson arrivals of the serving stream (seed 99) at two
+    rates through ctd_serve_*, p50/p99 completion latency and updates/s.
 
 Other workloads (--workload): `linear` (Fibonacci, Lucas and tribonacci,
-n = 1..50000, primes in [2^34, 2^36), one 2^30 segment of all three jobs per
-step), `smarandache` (base 10, n = 10..1000, all primes below 2^28, the whole
-configuration per step), `batched` (the 64-job mix through ctd_batch_run,
-against the same jobs one by one through ctd_run_plain) and `served` (Poisson
-arrivals through the ctd_serve_* server, p50/p99 latency per rate).
+n = 1..50000, primes in [2^34, 2^36)), `smarandache` (base 10, n = 10..1000,
+all primes below 2^28), `batched` and `served` alone.
 
   python bench.py [--gpus N --steps K --warmup W] [--workload W] [--impl reference]
 
@@ -76,32 +80,26 @@ PLAIN = {
 }
 FAMILY_NAMES = {0: "MERSENNE", 1: "PROTH", 2: "RIESEL", 3: "SMARANDACHE", 4: "FIBONACCI", 5: "LUCAS",
                 6: "PROTH_FIXED_N", 7: "RIESEL_FIXED_N", 8: "TRIBONACCI"}
-# Algorithmic integer-ALU operations per update, by family (32-bit ops of the
-# exact algorithm the kernel runs; multiplies, which go to the multiply pipe,
-# are listed separately):
-#  * doubling (Proth/Riesel/Mersenne): baby-step/giant-step blocks of 32
-#    terms through a per-prime target filter: per block a slot shift, a field
-#    shift, two funnel-shift bit tests, their AND and the OR into the vote of
-#    a group of eight blocks (6), the 32 exact compares on the ~5.5% of
-#    warp-blocks some lane passes (~2); the giant step (a 32-bit Montgomery
-#    reduction) and the hash multiply are on the multiply pipe -> 8/32;
-#  * fixed-n: the same filtered blocks, giant step a modular add (5) -> 13/32;
-#  * Fibonacci/Lucas (p < 2^40): lazily reduced blocks of 16 steps: a 64-bit
-#    add (2) and the zero-test compare (1) per step, plus one shift per state
-#    for the block-end reduction (2 per 16 steps) -> 3.125; the test's
-#    multiply and the reduction's multiply-adds run on the multiply pipe;
-#  * tribonacci (p < 2^40): blocks of 18 steps: a three-input 64-bit add (2)
-#    and the compare (1) per step, 3 shifts per block -> 57/18;
-#  * Smarandache (64-bit Shoup): adds/subtracts of x M + m - q p (4) and
-#    two low-word compares = 6, plus 9 32-bit multiplies.
-ALU_OPS_PER_UPDATE = {0: 8 / 32, 1: 8 / 32, 2: 8 / 32, 6: 13 / 32, 7: 13 / 32, 4: 50 / 16, 5: 50 / 16, 8: 57 / 18,
-                      3: 6}
-# DRAM bytes per prime of residue_kernel<PROTH> from one ncu capture on
-# [2^32, 2^32 + 2^27): 48,680,960 read + 3,608,320 written for 6,047,768
-# primes (each prime read once per launch; the writes are the factors buffer,
-# cleared at the start of the step, going back from L2), so a full launch's
-# traffic is this figure times its primes
-DRAM_BYTES_PER_PRIME = (48680960 + 3608320) / 6047768
+# Roofline inputs per workload (what the dominant launch executes):
+#  * proth -- the classified doubling launch (classify_kernel, regroup_kernel,
+#    class_walk_kernel): bound by integer issue slots.  Thread instructions
+#    and DRAM bytes per prime come from one ncu capture of the same three
+#    kernels on the 2^27-wide segment [2^32, 2^32 + 2^27) of this workload
+#    (6,047,768 primes; the capture's command is in the profile summary);
+#    the live launch time comes from CUDA events in this run.
+#  * smarandache -- the 32-bit Shoup step (p < 2^30): three 32-bit
+#    multiplies per update (the quotient's high half, x M and q p), against
+#    the integer multiply-add rate measured now;
+#  * linear -- the dominant tribonacci launch: lazily reduced blocks of 18
+#    steps, a three-input 64-bit add (2) and the compare (1) per step plus 3
+#    shifts per block = 57/18 ALU operations per update, against the ALU
+#    compare rate measured now.
+PROTH_NCU = {"primes": 6047768,
+             "thread_inst": {"classify_kernel": 1522607948 * 23.41, "regroup_kernel": 26304262 * 19.28,
+                             "class_walk_kernel": 3471573154 * 30.47},
+             "dram_bytes": (48.453888 + 0.735232 + 72.707328 + 12.887040 + 55.490304 + 8.239104) * 1e6}
+SMARANDACHE_MULS_PER_UPDATE = 3
+TRIBONACCI_ALU_OPS_PER_UPDATE = 57 / 18
 
 
 def mv_bound(y: int) -> int:
@@ -245,14 +243,15 @@ def run_reference(args, world, rank):
 
 def probe_peaks(device: int) -> dict:
     """Integer roofline denominators measured now by libctd_probe.so: the
-    ALU-pipe compare rate and the mixed add/xor integer rate."""
+    ALU-pipe compare rate, the mixed add/xor integer issue rate and the
+    32-bit multiply-add rate."""
     from cutrialdive_gb300._build import PROBE
 
-    out = {"alu": None, "int": None}
+    out = {"alu": None, "int": None, "imad": None}
     if not os.path.exists(PROBE):
         return out
     L = ctypes.CDLL(PROBE)
-    for key, fn in (("alu", "ctd_probe_alu_peak"), ("int", "ctd_probe_int_peak")):
+    for key, fn in (("alu", "ctd_probe_alu_peak"), ("int", "ctd_probe_int_peak"), ("imad", "ctd_probe_imad_peak")):
         f = getattr(L, fn, None)
         if f is None:
             continue
@@ -425,29 +424,49 @@ def run_ours(args, world, rank, local):
         return 0
 
     peaks = probe_peaks(local)
-    # the dominant kernel of the step and its roofline
+    # the dominant launch of the step and its roofline
     k = max(range(nj), key=lambda i: sum(job_ms[i]))
     fam = wl.jobs[k][0]
     launch_s = statistics.mean(job_ms[k]) * 1e-3
-    per_launch_updates = statistics.mean(nodd) * terms[k]
-    ops = ALU_OPS_PER_UPDATE[fam]
-    achieved = per_launch_updates * ops / launch_s
-    roofline = {
-        "bound": "int_alu", "kernel": f"residue_kernel<{FAMILY_NAMES[fam]}>",
-        "achieved": achieved / 1e9, "peak": (peaks["alu"] / 1e9) if peaks["alu"] else None, "unit": "Gop/s",
-        "frac": (achieved / peaks["alu"]) if peaks["alu"] else None,
-        "ops_per_update": ops, "launch_ms": launch_s * 1e3,
-        "peak_source": "measured now: libctd_probe predicate-compare chains (integer ALU pipe) on this GPU",
-        "int_issue_peak": (peaks["int"] / 1e9) if peaks["int"] else None,
-        "kernel_share": sum(job_ms[k]) / max(sum(sum(x) for x in job_ms) + sum(sieve_ms), 1e-9),
-    }
-    if fam == 1:
-        roofline["traffic"] = DRAM_BYTES_PER_PRIME * statistics.mean(nodd)
-        roofline["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one 2^27-segment launch "
-                                      "of this kernel, scaled by the primes per launch")
+    primes_launch = statistics.mean(nodd)
+    per_launch_updates = primes_launch * terms[k]
+    if wl.name == "proth":
+        inst = sum(PROTH_NCU["thread_inst"].values()) / PROTH_NCU["primes"] * primes_launch
+        achieved = inst / launch_s
+        roofline = {
+            "bound": "int_issue", "kernel": "classify_kernel<PROTH> + regroup_kernel + class_walk_kernel<PROTH>",
+            "achieved": achieved / 1e9, "peak": (peaks["int"] / 1e9) if peaks["int"] else None, "unit": "Ginst/s",
+            "frac": (achieved / peaks["int"]) if peaks["int"] else None,
+            "thread_instructions_per_update": inst / per_launch_updates, "launch_ms": launch_s * 1e3,
+            "achieved_source": "ncu thread instructions of the three kernels on a 2^27-segment of this workload, "
+                               "scaled by the primes per launch, over the CUDA-event launch time of this run",
+            "peak_source": "measured now: libctd_probe add/xor chains (integer issue rate) on this GPU",
+            "traffic": PROTH_NCU["dram_bytes"] / PROTH_NCU["primes"] * primes_launch,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the same capture, scaled by "
+                              "the primes per launch",
+            "algorithmic_bytes": 8 * primes_launch,
+        }
+    elif wl.name == "smarandache":
+        achieved = per_launch_updates * SMARANDACHE_MULS_PER_UPDATE / launch_s
+        roofline = {
+            "bound": "int_multiply", "kernel": "residue_kernel<SMARANDACHE> (32-bit Shoup step)",
+            "achieved": achieved / 1e9, "peak": (peaks["imad"] / 1e9) if peaks["imad"] else None,
+            "unit": "Gmul/s", "frac": (achieved / peaks["imad"]) if peaks["imad"] else None,
+            "muls_per_update": SMARANDACHE_MULS_PER_UPDATE, "launch_ms": launch_s * 1e3,
+            "peak_source": "measured now: libctd_probe 32-bit multiply-add chains on this GPU",
+            "traffic": None, "algorithmic_bytes": 8 * primes_launch,
+        }
     else:
-        roofline["traffic"] = None
-    roofline["algorithmic_bytes"] = 8 * statistics.mean(nodd)
+        achieved = per_launch_updates * TRIBONACCI_ALU_OPS_PER_UPDATE / launch_s
+        roofline = {
+            "bound": "int_alu", "kernel": f"residue_kernel<{FAMILY_NAMES[fam]}>",
+            "achieved": achieved / 1e9, "peak": (peaks["alu"] / 1e9) if peaks["alu"] else None, "unit": "Gop/s",
+            "frac": (achieved / peaks["alu"]) if peaks["alu"] else None,
+            "ops_per_update": TRIBONACCI_ALU_OPS_PER_UPDATE, "launch_ms": launch_s * 1e3,
+            "peak_source": "measured now: libctd_probe predicate-compare chains (integer ALU pipe) on this GPU",
+            "traffic": None, "algorithmic_bytes": 8 * primes_launch,
+        }
+    roofline["kernel_share"] = sum(job_ms[k]) / max(sum(sum(x) for x in job_ms) + sum(sieve_ms), 1e-9)
     per_job = {f"{FAMILY_NAMES[f].lower()}": {"ms_per_launch": statistics.mean(job_ms[i]),
                                              "updates_per_s": statistics.mean(nodd) * terms[i] /
                                              (statistics.mean(job_ms[i]) * 1e-3)}
@@ -482,10 +501,17 @@ def run_ours(args, world, rank, local):
         "clocks": clocks.summary(), "gpu_launches": int(launches),
         "updates": total_updates, "seconds": elapsed,
     }
+    ok = True
+    if wl.name == "proth" and not args.no_batched:
+        line["batched"] = measure_batched(args, eng, local)
+        ok &= line["batched"]["identical_outputs"] and line["batched"]["identical_to_reference"]
+    if wl.name == "proth" and not args.no_served:
+        line["served"] = measure_served(args, eng, local)
+        ok &= line["served"]["identical_to_reference"]
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
-    return 0
+    return 0 if ok else 1
 
 
 # ------------------------------------------------- batched / served workloads
@@ -514,102 +540,141 @@ def job_updates(eng, jobs) -> int:
     return total
 
 
-def run_batched(args, world, rank, local):
+def reference_mix_files() -> dict:
+    """The reference engine's factor files of the batched and serving mixes
+    on their fixture samples (tests/golden/golden_job_mixes.json)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from golden_util import expand, parse_args
+
+    with open(os.path.join(ROOT, "tests", "golden", "golden_job_mixes.json")) as fh:
+        data = json.load(fh)
+    out = {}
+    for name, g in data.items():
+        a = parse_args(g["args"])
+        out[name] = (a["f1"], expand(a["n0"], a["n1"], g["nonempty"]))
+    return out
+
+
+def restricted_text(buf, bound: int) -> str:
+    """A job's factor file keeping only the primes below `bound` (the factor
+    file of the same job on the TF range cut at `bound`)."""
+    res = buf.to_factoring_results()
+    n0 = res.n0()
+    lines = []
+    for i in range(len(res)):
+        ps = [p for p in res[i] if p < bound]
+        lines.append(f"{n0 + i} - " + ", ".join(map(str, ps)))
+    return "\n".join(lines) + "\n"
+
+
+def measure_batched(args, eng, local) -> dict:
+    """The batched mix through one ctd_batch_run against the same jobs one by
+    one through ctd_run_plain (both on 2^30 segments, both with host buffers
+    copied in and out inside the call)."""
     import torch
 
-    import cutrialdive_gb300 as ctd
     from cutrialdive_gb300 import _native as NAT
     from cutrialdive_gb300 import jobs as J
 
-    torch.cuda.set_device(local)
-    if rank != 0:
-        return 0
+    import cutrialdive_gb300 as ctd
+
     L = NAT.load()
-    eng = ctd.Engine(local)
     mix = J.batched_mix()
-    jobs = [j.ctd(MAXF, args.shrink) for j in mix]
+    jobs = [j.ctd(MAXF, args.batched_shrink) for j in mix]
     updates = job_updates(eng, jobs)
+    seg = 1 << 30
 
     def bufs():
         return [ctd.factors_buffer.empty(j.n0, j.n1 - j.n0, MAXF) for j in jobs]
 
     def batched_pass():
         b = bufs()
-        eng.batch_run(jobs, b, segment_length=1 << 30, use_graph=True)
+        eng.batch_run(jobs, b, segment_length=seg, use_graph=True)
         return b
 
     def sequential_pass():
         b = bufs()
         for j, x in zip(jobs, b):
-            eng.run_plain(j, x)
+            eng.run_plain(j, x, segment_length=seg)
         return b
 
-    for _ in range(args.warmup):
-        out_b = batched_pass()
+    out_b = batched_pass()  # warm-up: captures and instantiates the graph
+    g0 = eng.batch_graph_stats()
     l0 = L.ctd_kernel_launches()
+    steps = args.batched_steps
     with ClockSampler(local) as clocks:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for _ in range(args.steps):
+        for _ in range(steps):
             out_b = batched_pass()
         torch.cuda.synchronize()
-        tb = (time.perf_counter() - t0) / args.steps
-    launches = (L.ctd_kernel_launches() - l0) // args.steps
-    out_s = sequential_pass()  # warm
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    seq_steps = max(1, min(args.steps, 2))
-    for _ in range(seq_steps):
+        tb = (time.perf_counter() - t0) / steps
+        launches_b = (L.ctd_kernel_launches() - l0) // steps
+        l1 = L.ctd_kernel_launches()
+        t0 = time.perf_counter()
         out_s = sequential_pass()
-    torch.cuda.synchronize()
-    ts = (time.perf_counter() - t0) / seq_steps
+        torch.cuda.synchronize()
+        ts = time.perf_counter() - t0
+        launches_s = L.ctd_kernel_launches() - l1
+    g1 = eng.batch_graph_stats()
     identical = all(same_results(a, b) for a, b in zip(out_b, out_s))
-    h2d = sum((j.n1 - j.n0) * (4 + 8 * MAXF) for j in jobs)
-    line = {
-        "metric": METRIC, "value": updates / tb, "unit": "updates/s", "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * tb, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded job mix, seed 1234)",
-        "config": {"workload": BATCHED_WORKLOAD,
-                   "sample": f"each job's TF range cut to its first 1/{args.shrink}: [2^a, 2^a + 3*2^a/{args.shrink})",
-                   "step": "one ctd_batch_run over all 64 jobs (aligned 2^30 segments, one CUDA graph)",
-                   "l2": "prime lists of a segment (up to about 400 MB) exceed L2"},
+    ref = reference_mix_files()
+    checked = 0
+    ref_ok = True
+    for i, (j, buf) in enumerate(zip(jobs, out_b)):
+        name = f"batched{i:02d}"
+        if name in ref:
+            bound, text = ref[name]
+            ref_ok &= restricted_text(buf, bound) == text
+            checked += 1
+    hbytes = sum((j.n1 - j.n0) * (4 + 8 * MAXF) for j in jobs)
+    return {
+        "workload": BATCHED_WORKLOAD,
+        "sample": f"each job's TF range cut to its first 1/{args.batched_shrink}: "
+                  f"[2^a, 2^a + 3*2^a/{args.batched_shrink})",
         "updates_per_step": updates,
-        "sequential": {"value": updates / ts, "ms_per_step": 1e3 * ts, "steps": seq_steps,
-                       "api": "ctd_run_plain per job, default 2^26 segments, same host buffers"},
-        "batched_over_sequential": ts / tb, "identical_outputs": identical,
-        "e2e": {"value": updates / tb, "unit": "updates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
-                "api": "ctd_batch_run with host factors buffers (copies inside the call)"},
-        "clocks": clocks.summary(), "gpu_launches": int(launches),
+        "value": updates / tb, "unit": "updates/s", "ms_per_step": 1e3 * tb, "steps": steps, "warmup": 1,
+        "api": "one ctd_batch_run of all 64 jobs (2^30 segments, the schedule replayed as one CUDA graph), host "
+               "factors buffers copied in and out inside the call",
+        "sequential": {"value": updates / ts, "ms_per_step": 1e3 * ts, "steps": 1, "gpu_launches": int(launches_s),
+                       "api": "ctd_run_plain per job, 2^30 segments, the same host buffers"},
+        "batched_over_sequential": ts / tb,
+        "identical_outputs": bool(identical),
+        "identical_to_reference": bool(ref_ok and checked == len(jobs)),
+        "reference_check": f"{checked} jobs: factor lines with p < 2^a + 2^24 equal the reference engine's files "
+                           "(tests/golden/golden_job_mixes.json)",
+        "graph": {k: g1[k] - g0[k] for k in g1},
+        "gpu_launches": int(launches_b),
+        "h2d_bytes_per_step": hbytes, "d2h_bytes_per_step": hbytes,
+        "clocks": clocks.summary(),
     }
-    print(json.dumps(line), flush=True)
-    return 0 if identical else 1
 
 
-def run_served(args, world, rank, local):
+def measure_served(args, eng, local) -> dict:
+    """Poisson arrivals of the serving stream through ctd_serve_*: per rate,
+    the jobs arriving in the first `window` seconds, each job's TF range cut
+    to its first 1/served_shrink; p50/p99 from arrival to fetched result."""
     import numpy as np
-    import torch
 
     import cutrialdive_gb300 as ctd
     from cutrialdive_gb300 import _native as NAT
     from cutrialdive_gb300 import jobs as J
 
-    torch.cuda.set_device(local)
-    if rank != 0:
-        return 0
     L = NAT.load()
-    eng = ctd.Engine(local)
     rates = [float(r) for r in args.rates.split(",")]
+    ref = reference_mix_files()
     sweep = []
+    ref_ok, checked = True, 0
     l0 = L.ctd_kernel_launches()
     with ClockSampler(local) as clocks:
         for rate in rates:
             mix, arrivals = J.served_mix(rate)
             count = min(len(mix), max(1, int(rate * args.window)))
-            jobs = [j.ctd(MAXF, args.shrink) for j in mix[:count]]
+            jobs = [j.ctd(MAXF, args.served_shrink) for j in mix[:count]]
             arrivals = arrivals[:count]
             updates = job_updates(eng, jobs)
             srv = ctd.Server(eng, memory_budget=160 << 30, max_active=256, segment_length=1 << 30)
-            lat, ids, i = [], {}, 0
+            lat, ids, i, results = [], {}, 0, {}
             t0 = time.perf_counter()
             while len(lat) < count:
                 now = time.perf_counter() - t0
@@ -619,33 +684,83 @@ def run_served(args, world, rank, local):
                 st = srv.status()
                 if st["active"] or st["queued"]:
                     for jid in srv.tick():
-                        srv.fetch(jid)
-                        lat.append(time.perf_counter() - t0 - arrivals[ids.pop(jid)])
+                        k = ids.pop(jid)
+                        results[k] = srv.fetch(jid)
+                        lat.append(time.perf_counter() - t0 - arrivals[k])
                 elif i < count:
-                    time.sleep(max(0.0, min(arrivals[i] - now, 0.05)))
+                    time.sleep(max(0.0, min(arrivals[i] - now, 0.02)))
             span = time.perf_counter() - t0
             srv.close()
+            for k, buf in results.items():
+                name = f"served{k:03d}"
+                if name in ref:
+                    bound, text = ref[name]
+                    ref_ok &= restricted_text(buf, bound) == text
+                    checked += 1
             sweep.append({"rate_jobs_s": rate, "jobs": count, "p50_s": float(np.percentile(lat, 50)),
                           "p99_s": float(np.percentile(lat, 99)), "updates": updates,
                           "updates_per_s": updates / span, "seconds": span})
-    launches = L.ctd_kernel_launches() - l0
-    best = max(sweep, key=lambda r: r["updates_per_s"])
+    return {
+        "workload": "Serving: Poisson arrival stream from the batched distribution (seed 99), admission by a "
+                    "160 GB device-memory budget",
+        "sample": f"each job's TF range cut to its first 1/{args.served_shrink}; at each rate the jobs arriving in "
+                  f"the first {args.window:g} s",
+        "server": "ctd_serve_* with max_active 256, 2^30 segments per tick, ticks queued up to two ahead",
+        "sweep": sweep,
+        "identical_to_reference": bool(ref_ok and checked > 0),
+        "reference_check": f"{checked} jobs among the stream's first 200: factor lines with p < 2^a + 2^22 equal "
+                           "the reference engine's files (tests/golden/golden_job_mixes.json)",
+        "gpu_launches": int(L.ctd_kernel_launches() - l0),
+        "clocks": clocks.summary(),
+    }
+
+
+def run_batched(args, world, rank, local):
+    import torch
+
+    import cutrialdive_gb300 as ctd
+
+    torch.cuda.set_device(local)
+    if rank != 0:
+        return 0
+    eng = ctd.Engine(local)
+    b = measure_batched(args, eng, local)
+    line = {
+        "metric": METRIC, "value": b["value"], "unit": "updates/s", "n_gpus": 1, "steps": b["steps"],
+        "warmup": b["warmup"], "ms_per_step": b["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded job mix, seed 1234)",
+        "config": {"workload": b["workload"], "sample": b["sample"]},
+        "batched": b, "clocks": b["clocks"], "gpu_launches": b["gpu_launches"],
+        "e2e": {"value": b["value"], "unit": "updates/s", "h2d_bytes_per_step": b["h2d_bytes_per_step"],
+                "d2h_bytes_per_step": b["d2h_bytes_per_step"], "api": b["api"]},
+    }
+    print(json.dumps(line), flush=True)
+    return 0 if b["identical_outputs"] and b["identical_to_reference"] else 1
+
+
+def run_served(args, world, rank, local):
+    import torch
+
+    import cutrialdive_gb300 as ctd
+
+    torch.cuda.set_device(local)
+    if rank != 0:
+        return 0
+    eng = ctd.Engine(local)
+    sv = measure_served(args, eng, local)
+    best = max(sv["sweep"], key=lambda r: r["updates_per_s"])
     line = {
         "metric": METRIC + "; p50/p99 job latency", "value": best["updates_per_s"], "unit": "updates/s",
-        "n_gpus": 1, "steps": len(rates), "warmup": 0, "ms_per_step": 1e3 * best["seconds"],
+        "n_gpus": 1, "steps": len(sv["sweep"]), "warmup": 0, "ms_per_step": 1e3 * best["seconds"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic (Poisson arrivals of the seeded job mix, seed 99)",
-        "config": {"workload": "Serving: Poisson arrival stream from the batched distribution (seed 99), "
-                               "admission by a 160 GB HBM budget",
-                   "sample": f"each job's TF range cut to its first 1/{args.shrink}; at each rate the jobs "
-                             f"arriving in the first {args.window:g} s (at most 2000)",
-                   "server": "ctd_serve_* with max_active 256, 2^30 segments per tick"},
-        "sweep": sweep, "clocks": clocks.summary(), "gpu_launches": int(launches),
+        "config": {"workload": sv["workload"], "sample": sv["sample"], "server": sv["server"]},
+        "served": sv, "clocks": sv["clocks"], "gpu_launches": sv["gpu_launches"],
         "e2e": {"value": best["updates_per_s"], "unit": "updates/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0, "api": "ctd_serve_submit/tick/fetch (host buffers)"},
     }
     print(json.dumps(line), flush=True)
-    return 0
+    return 0 if sv["identical_to_reference"] else 1
 
 
 def main() -> int:
@@ -664,9 +779,15 @@ def main() -> int:
                     help="proth: the plain single-job line (default); linear: Fibonacci, Lucas and tribonacci back "
                          "to back; smarandache: the CPU-runnable plain configuration; batched: the 64-job mix "
                          "through ctd_batch_run against the same jobs one by one; served: the Poisson serving sweep")
-    ap.add_argument("--shrink", type=int, default=256, help="batched/served: keep the first 1/shrink of each TF range")
-    ap.add_argument("--rates", default="1,5,10,25,50", help="served: arrival rates in jobs/s")
-    ap.add_argument("--window", type=float, default=10.0, help="served: seconds of arrivals per rate")
+    ap.add_argument("--batched-shrink", type=int, default=64,
+                    help="batched: keep the first 1/shrink of each job's TF range")
+    ap.add_argument("--batched-steps", type=int, default=2, help="batched: timed passes")
+    ap.add_argument("--served-shrink", type=int, default=256,
+                    help="served: keep the first 1/shrink of each job's TF range")
+    ap.add_argument("--rates", default="10,50", help="served: arrival rates in jobs/s")
+    ap.add_argument("--window", type=float, default=6.0, help="served: seconds of arrivals per rate")
+    ap.add_argument("--no-batched", action="store_true", help="default line without the batched measurement")
+    ap.add_argument("--no-served", action="store_true", help="default line without the served measurement")
     ap.add_argument("--cpu-seconds", type=float, default=2.0,
                     help="--impl reference: seconds of CPU work per step (a bounded sample of the step)")
     args = ap.parse_args()

@@ -51,6 +51,28 @@ CTD_HD void crt_merge(PowerClass &c, uint32_t j, uint32_t q)
     c.M *= q;
 }
 
+// The classifier's multiplications go through one out-of-line function on
+// the device: inlined, its ~140 Montgomery products made a kernel large
+// enough that warps stalled on instruction fetch (ncu: "no instruction"
+// the top stall).
+#ifdef __CUDA_ARCH__
+__device__ __noinline__ uint64_t powres_mul(uint64_t a, uint64_t b, uint64_t p, uint64_t pinv)
+{
+    Mont m;
+    m.p = p;
+    m.pinv = pinv;
+    return m.mul(a, b);
+}
+#else
+inline uint64_t powres_mul(uint64_t a, uint64_t b, uint64_t p, uint64_t pinv)
+{
+    Mont m;
+    m.p = p;
+    m.pinv = pinv;
+    return m.mul(a, b);
+}
+#endif
+
 // base^e (base in Montgomery form, e small)
 CTD_HD uint64_t small_pow(const Mont &m, uint64_t base, uint32_t e)
 {
@@ -88,9 +110,10 @@ struct Pow105 {
 };
 CTD_HD Pow105 pow105(const Mont &m, uint64_t x)
 {
-    const uint64_t x2 = m.mul(x, x), x3 = m.mul(x2, x), x5 = m.mul(x3, x2), x7 = m.mul(x5, x2);
-    const uint64_t x10 = m.mul(x5, x5), x15 = m.mul(x10, x5), x14 = m.mul(x7, x7), x21 = m.mul(x14, x7);
-    const uint64_t x35 = m.mul(x21, x14), x70 = m.mul(x35, x35), x105 = m.mul(x70, x35);
+    auto mul = [&](uint64_t a, uint64_t b) { return powres_mul(a, b, m.p, m.pinv); };
+    const uint64_t x2 = mul(x, x), x3 = mul(x2, x), x5 = mul(x3, x2), x7 = mul(x5, x2);
+    const uint64_t x10 = mul(x5, x5), x15 = mul(x10, x5), x14 = mul(x7, x7), x21 = mul(x14, x7);
+    const uint64_t x35 = mul(x21, x14), x70 = mul(x35, x35), x105 = mul(x70, x35);
     return Pow105{x15, x21, x35, x105};
 }
 
@@ -115,15 +138,25 @@ CTD_HD PowerClass doubling_class(const Mont &m, uint64_t k, bool negate)
     e0 = f3 ? e0 / 3 : e0;
     e0 = f5 ? e0 / 5 : e0;
     e0 = f7 ? e0 / 7 : e0;
-    // A = 2^-e0 = 2^(p - 1 - e0); B = wt^e0 = (-+1)^e0 k^e0 by left-to-right
-    // powering with Shoup multiplications by the plain k
-    const uint64_t A = m.pow2(p1 - e0);
+    auto mul = [&](uint64_t a, uint64_t b) { return powres_mul(a, b, p, m.pinv); };
+    // A = 2^-e0 = 2^(p - 1 - e0) (left-to-right, a set bit a doubling); B =
+    // wt^e0 = (-+1)^e0 k^e0 by left-to-right powering with Shoup
+    // multiplications by the plain k
+    uint64_t A = m.one;
+    {
+        const uint64_t e = p1 - e0;
+        for (int b = 63 - clz64(e); b >= 0; --b) {
+            A = mul(A, A);
+            if ((e >> b) & 1)
+                A = m.dbl(A);
+        }
+    }
     uint64_t B = m.one;
     {
         const uint64_t kr = k < p ? k : k % p;
         const uint64_t ks = m.shoup(kr);
         for (int b = 63 - clz64(e0); b >= 0; --b) {
-            B = m.mul(B, B);
+            B = mul(B, B);
             if ((e0 >> b) & 1)
                 B = shoup_mul(B, kr, ks, p);
         }
@@ -145,8 +178,8 @@ CTD_HD PowerClass doubling_class(const Mont &m, uint64_t k, bool negate)
         bool found = zs == m.one;
 #pragma unroll
         for (int t = 1; t <= POWRES_MAX_2EXP; ++t) {
-            zs = m.mul(zs, zs);
-            ys = m.mul(ys, ys);
+            zs = mul(zs, zs);
+            ys = mul(ys, ys);
             if (!found && t <= u) {
                 i = t;
                 y_ok = ys == m.one;
@@ -162,7 +195,7 @@ CTD_HD PowerClass doubling_class(const Mont &m, uint64_t k, bool negate)
         for (uint32_t jj = 0; jj < (1u << POWRES_MAX_2EXP); ++jj) {
             if (jj < (1u << i) && t == y)
                 j = jj;
-            t = m.mul(t, z);
+            t = mul(t, z);
         }
         c.M = 1u << i;
         c.r = j;
@@ -171,7 +204,7 @@ CTD_HD PowerClass doubling_class(const Mont &m, uint64_t k, bool negate)
     uint64_t A2 = A, B2 = B;  // A^(2^u), B^(2^u): loops of fixed length
 #pragma unroll
     for (int t = 0; t < POWRES_MAX_2EXP; ++t) {
-        const uint64_t a2 = m.mul(A2, A2), b2 = m.mul(B2, B2);
+        const uint64_t a2 = mul(A2, A2), b2 = mul(B2, B2);
         A2 = t < u ? a2 : A2;
         B2 = t < u ? b2 : B2;
     }
@@ -192,7 +225,7 @@ CTD_HD PowerClass doubling_class(const Mont &m, uint64_t k, bool negate)
         for (uint32_t jj = 0; jj < q; ++jj) {
             if (t == y)
                 j = jj;
-            t = m.mul(t, z);
+            t = mul(t, z);
         }
         if (j >= q)  // cannot happen for prime p (y is a q-th root of unity)
             return PowerClass{1, 0};

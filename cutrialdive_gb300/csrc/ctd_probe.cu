@@ -69,9 +69,71 @@ __global__ void __launch_bounds__(256) isetp_chains(uint32_t *out, uint32_t iter
         out[blockIdx.x] = flags;
 }
 
+// Integer multiply pipe: eight independent chains of 32-bit multiply-adds
+// (IMAD, a = a * y + z), the instruction the Smarandache steps are built
+// from; 128 multiply-adds per iteration.
+__global__ void __launch_bounds__(256) imad_chains(uint32_t *out, uint32_t iters, uint32_t y, uint32_t z)
+{
+    uint32_t a0 = threadIdx.x, a1 = a0 ^ 0x9e3779b9u, a2 = a0 + 7u, a3 = a0 * 3u;
+    uint32_t a4 = a0 ^ y, a5 = a0 + z, a6 = a0 ^ 0x85ebca6bu, a7 = a0 + 0x27d4eb2fu;
+    for (uint32_t i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            a0 = a0 * y + z;
+            a1 = a1 * y + z;
+            a2 = a2 * y + z;
+            a3 = a3 * y + z;
+            a4 = a4 * y + z;
+            a5 = a5 * y + z;
+            a6 = a6 * y + z;
+            a7 = a7 * y + z;
+        }
+    }
+    uint32_t s = a0 ^ a1 ^ a2 ^ a3 ^ a4 ^ a5 ^ a6 ^ a7;
+    if (s == 0x12345678u)  // practically never; keeps the chains live
+        out[blockIdx.x] = s;
+}
+
 }  // namespace
 
 extern "C" {
+
+// 32-bit integer multiply-adds per second over a ~0.5 s run on `device`
+// (8 chains x 16 unrolled x iters per thread).  Returns 0 on success.
+int ctd_probe_imad_peak(int device, double *imad_per_s, double *seconds)
+{
+    if (cudaSetDevice(device) != cudaSuccess)
+        return -2;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    uint32_t *out = nullptr;
+    const int block = 256, grid = sms * 8;
+    if (cudaMalloc(&out, grid * sizeof(uint32_t)) != cudaSuccess)
+        return -3;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const uint32_t iters = 2048;
+    imad_chains<<<grid, block>>>(out, 64, 0x1234567u, 0x89abcdefu);  // warm-up
+    cudaEventRecord(e0);
+    const int reps = 8;
+    for (int r = 0; r < reps; ++r)
+        imad_chains<<<grid, block>>>(out, iters, 0x1234567u + 2 * r, 0x89abcdefu);
+    cudaEventRecord(e1);
+    cudaError_t err = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (err != cudaSuccess || ms <= 0.f)
+        return -2;
+    const double instr = 8.0 * 16 * (double)iters * block * grid * reps;
+    *imad_per_s = instr / (ms * 1e-3);
+    if (seconds)
+        *seconds = ms * 1e-3;
+    return 0;
+}
 
 // Predicate compares per second (ALU pipe) over a ~0.5 s run on `device`
 // (128 compares per iteration; the dozen or/select/add/loop instructions

@@ -1493,25 +1493,48 @@ __device__ __forceinline__ void run_item(const JobView &job, uint64_t p, uint64_
         run_peano(job, p, s, e);
 }
 
+// one (prime, tile) item: item k is tile k mod tiles of prime k / tiles
 template <uint32_t FAM>
-__global__ void __launch_bounds__(256, min_ctas_per_sm(FAM))
-residue_kernel(JobView job, const uint64_t *__restrict__ primes, uint64_t nprimes)
+__device__ __forceinline__ void residue_item(const JobView &job, const uint64_t *__restrict__ primes, uint64_t k)
 {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    const uint64_t first = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (job.tiles == 1) {
-        for (uint64_t i = first; i < nprimes; i += stride)
-            run_item<FAM>(job, primes[i], job.n0, job.n1);
+        run_item<FAM>(job, primes[k], job.n0, job.n1);
         return;
     }
+    const uint64_t i = k / job.tiles;
+    const uint64_t t = k - i * job.tiles;
+    const uint64_t s = job.n0 + t * job.tile_len;
+    const uint64_t e = s + job.tile_len < job.n1 ? s + job.tile_len : job.n1;
+    if (s < e)
+        run_item<FAM>(job, primes[i], s, e);
+}
+
+// Persistent grid.  With a work counter (zero at launch) each warp takes
+// the next 32 items until none are left, so an SM that runs slower than the
+// others -- or holds the costliest primes -- simply takes fewer items and
+// every SM finishes within one item of the others; without one, threads
+// stride over the items.
+template <uint32_t FAM>
+__global__ void __launch_bounds__(256, min_ctas_per_sm(FAM))
+residue_kernel(JobView job, const uint64_t *__restrict__ primes, uint64_t nprimes, unsigned long long *next)
+{
     const uint64_t items = nprimes * job.tiles;
-    for (uint64_t w = first; w < items; w += stride) {
-        uint64_t i = w / job.tiles;
-        uint64_t t = w - i * job.tiles;
-        uint64_t s = job.n0 + t * job.tile_len;
-        uint64_t e = s + job.tile_len < job.n1 ? s + job.tile_len : job.n1;
-        if (s < e)
-            run_item<FAM>(job, primes[i], s, e);
+    if (!next) {
+        const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+        for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < items; k += stride)
+            residue_item<FAM>(job, primes, k);
+        return;
+    }
+    const uint32_t lane = threadIdx.x & 31u;
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0)
+            base = atomicAdd(next, 32ull);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= items)
+            break;
+        if (base + lane < items)
+            residue_item<FAM>(job, primes, base + lane);
     }
 }
 
@@ -2002,13 +2025,15 @@ int prepare_residue_tables(int device, std::string &err)
 // ----------------------------------------------------------- launchers
 template <uint32_t FAM>
 static cudaError_t launch_fam(const JobView &v, const uint64_t *d_primes, uint64_t n, int grid, int block,
-                              cudaStream_t st)
+                              cudaStream_t st, unsigned long long *next)
 {
     const size_t sm = smem_bytes<FAM>(block);
     cudaError_t e = allow_smem(residue_kernel<FAM>, sm);
+    if (e == cudaSuccess && next)
+        e = cudaMemsetAsync(next, 0, sizeof(*next), st);
     if (e != cudaSuccess)
         return e;
-    residue_kernel<FAM><<<grid, block, sm, st>>>(v, d_primes, n);
+    residue_kernel<FAM><<<grid, block, sm, st>>>(v, d_primes, n, next);
     return cudaGetLastError();
 }
 
@@ -2121,18 +2146,26 @@ int launch_residues(const JobView &view, const uint64_t *d_primes, uint64_t npri
         default: return launch_classified<MERSENNE>(view, d_primes, nprimes, stream, scratch, err);
         }
     }
+    // the work counter of the persistent grid (the context's scratch)
+    unsigned long long *next = nullptr;
+    if (scratch) {
+        int rc0 = ensure_class_scratch(scratch, 0, err);
+        if (rc0)
+            return rc0;
+        next = &scratch->counters->next;
+    }
     cudaError_t rc;
     switch (view.family) {
-    case MERSENNE: rc = launch_fam<MERSENNE>(view, d_primes, nprimes, grid, block, stream); break;
-    case PROTH: rc = launch_fam<PROTH>(view, d_primes, nprimes, grid, block, stream); break;
-    case RIESEL: rc = launch_fam<RIESEL>(view, d_primes, nprimes, grid, block, stream); break;
-    case SMARANDACHE: rc = launch_fam<SMARANDACHE>(view, d_primes, nprimes, grid, block, stream); break;
-    case FIBONACCI: rc = launch_fam<FIBONACCI>(view, d_primes, nprimes, grid, block, stream); break;
-    case LUCAS: rc = launch_fam<LUCAS>(view, d_primes, nprimes, grid, block, stream); break;
-    case PROTH_FIXED_N: rc = launch_fam<PROTH_FIXED_N>(view, d_primes, nprimes, grid, block, stream); break;
-    case RIESEL_FIXED_N: rc = launch_fam<RIESEL_FIXED_N>(view, d_primes, nprimes, grid, block, stream); break;
-    case TRIBONACCI: rc = launch_fam<TRIBONACCI>(view, d_primes, nprimes, grid, block, stream); break;
-    case PEANO: rc = launch_fam<PEANO>(view, d_primes, nprimes, grid, block, stream); break;
+    case MERSENNE: rc = launch_fam<MERSENNE>(view, d_primes, nprimes, grid, block, stream, next); break;
+    case PROTH: rc = launch_fam<PROTH>(view, d_primes, nprimes, grid, block, stream, next); break;
+    case RIESEL: rc = launch_fam<RIESEL>(view, d_primes, nprimes, grid, block, stream, next); break;
+    case SMARANDACHE: rc = launch_fam<SMARANDACHE>(view, d_primes, nprimes, grid, block, stream, next); break;
+    case FIBONACCI: rc = launch_fam<FIBONACCI>(view, d_primes, nprimes, grid, block, stream, next); break;
+    case LUCAS: rc = launch_fam<LUCAS>(view, d_primes, nprimes, grid, block, stream, next); break;
+    case PROTH_FIXED_N: rc = launch_fam<PROTH_FIXED_N>(view, d_primes, nprimes, grid, block, stream, next); break;
+    case RIESEL_FIXED_N: rc = launch_fam<RIESEL_FIXED_N>(view, d_primes, nprimes, grid, block, stream, next); break;
+    case TRIBONACCI: rc = launch_fam<TRIBONACCI>(view, d_primes, nprimes, grid, block, stream, next); break;
+    case PEANO: rc = launch_fam<PEANO>(view, d_primes, nprimes, grid, block, stream, next); break;
     default: err = "unknown sequence family"; return CTD_ERR_INVALID_ARGUMENT;
     }
     if (rc != cudaSuccess) {

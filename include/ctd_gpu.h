@@ -186,7 +186,9 @@ int ctd_sieve_device(ctd_ctx *ctx, uint64_t lo, uint64_t hi, uint64_t *d_out, ui
  * pushing hits into a device factors buffer (slots past a term's count
  * zero, as for ctd_run_plain).  The unit that
  * trial_div_by_odd_primes<Seq, 1, ...> implements (src/trial_factoring.cuh:156-228).
- * Asynchronous on `stream`. */
+ * Asynchronous on `stream`; the launches use the context's scratch (work
+ * counter, class buffers), so calls on one context must not overlap on
+ * different streams. */
 int ctd_residues_device(ctd_ctx *ctx, const ctd_job *job, const uint64_t *d_primes, uint64_t nprimes,
                         uint32_t *d_counts, uint64_t *d_factors, void *stream);
 

@@ -25,3 +25,25 @@ def test_reference_arm_json_line(workload):
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["value"] == d["value"]
     assert d["config"]["workload"]
+
+
+def test_restricted_factor_files_match_reference_fixtures():
+    """bench.py checks batched and served results against the reference
+    engine's files of a smaller TF range by dropping the primes above it:
+    the oracle's result on a wider range, cut that way, reproduces the
+    reference file of the narrower one."""
+    sys.path.insert(0, ROOT)
+    import bench
+    import oracle
+    from cutrialdive_gb300 import factors_buffer
+
+    ref = bench.reference_mix_files()
+    assert len(ref) == 264
+    bound, text = ref["served159"]
+    import golden_util
+
+    with open(os.path.join(ROOT, "tests", "golden", "golden_job_mixes.json")) as fh:
+        a = golden_util.parse_args(json.load(fh)["served159"]["args"])
+    wide = oracle.trial_factor(a["family"], a["param"], a["n0"], a["n1"], a["f0"], a["f1"] + (1 << 20), 32)
+    buf = factors_buffer(a["n0"], 32, wide.counts, wide.factors)
+    assert bench.restricted_text(buf, bound) == text
