@@ -73,6 +73,8 @@ SIGNATURES = {
     "ctd_serve_status": (i32, [vp, ctypes.POINTER(u32), ctypes.POINTER(u32), p64]),
     "ctd_get_tuning": (i32, [vp, u32, ctypes.POINTER(CtdTuning)]),
     "ctd_set_tuning": (i32, [vp, u32, ctypes.POINTER(CtdTuning)]),
+    "ctd_get_tuning_for": (i32, [vp, u32, u32, ctypes.POINTER(CtdTuning)]),
+    "ctd_set_tuning_for": (i32, [vp, u32, u32, ctypes.POINTER(CtdTuning)]),
     "ctd_autotune": (i32, [vp, ctypes.POINTER(CtdJob), ctypes.c_double, ctypes.POINTER(CtdTuning)]),
 }
 

@@ -365,6 +365,20 @@ class Engine:
         t = N.CtdTuning(**{k: int(v) for k, v in tuning.items()})
         self._check(self._L.ctd_set_tuning(self._h, family, ctypes.byref(t)), "ctd_set_tuning")
 
+    def get_tuning_for(self, family: int, prime_bits: int) -> dict:
+        """Parameters in force for a family at primes of `prime_bits` bits (ctd_get_tuning_for)."""
+        t = N.CtdTuning()
+        self._check(self._L.ctd_get_tuning_for(self._h, family, prime_bits, ctypes.byref(t)), "ctd_get_tuning_for")
+        return t.as_dict()
+
+    def set_tuning_for(self, family: int, prime_bits: int, tuning: dict | None) -> None:
+        """Sets (or with None clears) a family's entry for one prime width (ctd_set_tuning_for)."""
+        if tuning is None:
+            self._check(self._L.ctd_set_tuning_for(self._h, family, prime_bits, None), "ctd_set_tuning_for")
+            return
+        t = N.CtdTuning(**{k: int(v) for k, v in tuning.items()})
+        self._check(self._L.ctd_set_tuning_for(self._h, family, prime_bits, ctypes.byref(t)), "ctd_set_tuning_for")
+
     def autotune(self, job: N.CtdJob, budget_s: float = 2.0) -> dict:
         """Measures and applies the fastest parameters for the job's family (ctd_autotune)."""
         t = N.CtdTuning()

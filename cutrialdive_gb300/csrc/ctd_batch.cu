@@ -6,9 +6,11 @@
 //
 // * ctd_batch_run walks the union of the jobs' prime ranges segment by
 //   segment ("chunk-major"): each aligned segment is sieved once and
-//   consumed by every job whose range covers it, in ONE persistent walk
-//   launch over (job, 32 primes, index tile) work items of every family
-//   (launch_batch, ctd_residue.cu).  The whole schedule -- sieves, class and
+//   consumed by every job whose range covers it: persistent walk launches
+//   over (job, 32 primes, index tile) work items, one per walk group present
+//   (the doubling families, Smarandache, the rest: each group's kernel has
+//   the occupancy and registers its families need; launch_batch,
+//   ctd_residue.cu).  The whole schedule -- sieves, class and
 //   plan kernels, walks -- is captured once into a CUDA graph; a later call
 //   with the same schedule replays it, one with the same shape updates the
 //   instantiated graph in place, and the device buffers stay with the
@@ -97,7 +99,7 @@ BatchJob batch_job_of(ctd_ctx *ctx, const ctd_job &j, uint32_t *counts, uint64_t
 {
     BatchJob b{};
     JobView &v = b.view;
-    const ctd_tuning t = ctx_tuning(ctx, j.family);
+    const ctd_tuning t = ctx_tuning(ctx, j.family, j.f0);
     v.family = j.family;
     v.variant = t.variant;
     v.classify_min = t.classify_min ? t.classify_min : DEFAULT_CLASSIFY_MIN;
@@ -105,7 +107,8 @@ BatchJob batch_job_of(ctd_ctx *ctx, const ctd_job &j, uint32_t *counts, uint64_t
     v.n0 = j.n0;
     v.n1 = j.n1;
     const uint64_t N = j.n1 - j.n0;
-    const uint64_t lim = tile_limit(j.family);
+    // index tiles: the family's limit, raised to the tuned shortest tile
+    const uint64_t lim = tile_limit(j.family) == ~0ull ? ~0ull : std::max<uint64_t>(tile_limit(j.family), t.min_tile);
     v.tiles = (uint32_t)(N <= lim ? 1 : std::min<uint64_t>((N + lim - 1) / lim, 1u << 20));
     v.tile_len = (N + v.tiles - 1) / v.tiles;
     v.tiles = (uint32_t)((N + v.tile_len - 1) / v.tile_len);
@@ -174,6 +177,7 @@ struct BatchCache {
     size_t bucket_cap = 0;
     cudaGraphExec_t exec = nullptr;
     uint64_t key = 0;
+    uint64_t graph_launches = 0;  // kernel launches in the captured schedule
     uint64_t replays = 0, updates = 0, instantiations = 0;
 
     BatchScratch scratch(uint32_t nactive) const
@@ -216,8 +220,26 @@ namespace {
 struct Segment {
     uint64_t lo, hi;
     uint32_t first, count;
+    uint32_t gcount[BATCH_GROUPS];  // jobs per walk group (the slice is group-major)
     bool any_classified;
 };
+
+// a segment's active jobs ordered walk group by walk group, heaviest work
+// per prime first within a group (the walks hand out items in this order)
+template <class Terms, class Family>
+void order_active(std::vector<uint32_t> &act, uint32_t gcount[BATCH_GROUPS], Terms terms, Family family)
+{
+    std::stable_sort(act.begin(), act.end(), [&](uint32_t x, uint32_t y) {
+        const int gx = batch_group(family(x)), gy = batch_group(family(y));
+        if (gx != gy)
+            return gx < gy;
+        return (double)terms(x) * term_cost(family(x)) > (double)terms(y) * term_cost(family(y));
+    });
+    for (int g = 0; g < BATCH_GROUPS; ++g)
+        gcount[g] = 0;
+    for (uint32_t x : act)
+        ++gcount[batch_group(family(x))];
+}
 
 // The segments of [lo, hi) aligned to S that some job covers, and their
 // active jobs; also the largest per-segment needs for sizing scratch.
@@ -254,19 +276,18 @@ Schedule plan_schedule(const std::vector<BatchJob> &hjobs, const ctd_job *jobs, 
             }
         if (act.empty())
             continue;
-        // heaviest work per prime first: the walk hands out items in this order
-        std::stable_sort(act.begin(), act.end(), [&](uint32_t x, uint32_t y) {
-            return (double)(jobs[x].n1 - jobs[x].n0) * term_cost(jobs[x].family) >
-                   (double)(jobs[y].n1 - jobs[y].n0) * term_cost(jobs[y].family);
-        });
         for (size_t b = 0; b < act.size(); b += MAX_ACTIVE_PER_LAUNCH) {
             Segment part = sg;
             part.first = (uint32_t)sc.active.size();
             part.count = (uint32_t)std::min<size_t>(MAX_ACTIVE_PER_LAUNCH, act.size() - b);
+            std::vector<uint32_t> slice(act.begin() + b, act.begin() + b + part.count);
+            order_active(
+                slice, part.gcount, [&](uint32_t x) { return jobs[x].n1 - jobs[x].n0; },
+                [&](uint32_t x) { return jobs[x].family; });
             part.any_classified = false;
-            for (uint32_t q = 0; q < part.count; ++q)
-                part.any_classified |= hjobs[act[b + q]].classified != 0;
-            sc.active.insert(sc.active.end(), act.begin() + b, act.begin() + b + part.count);
+            for (uint32_t x : slice)
+                part.any_classified |= hjobs[x].classified != 0;
+            sc.active.insert(sc.active.end(), slice.begin(), slice.end());
             sc.max_active = std::max(sc.max_active, part.count);
             sc.segs.push_back(part);
         }
@@ -361,7 +382,7 @@ int ctd_batch_run(ctd_ctx *ctx, const ctd_job *jobs, uint32_t njobs, uint32_t *c
             const uint64_t *d_count = nullptr;
             int rc = sieve_odd_async(ctx_workspace(ctx), g.lo, g.hi, bc.primes, bc.primes_cap, &d_count, st, err);
             if (!rc)
-                rc = launch_batch(bc.jobs, bc.active + g.first, g.count, g.any_classified, bc.primes, d_count, g.lo,
+                rc = launch_batch(bc.jobs, bc.active + g.first, g.gcount, g.any_classified, bc.primes, d_count, g.lo,
                                   g.hi, bc.scratch(g.count), ctx_sm_count(ctx), st, err);
             if (rc)
                 return rc;
@@ -390,12 +411,15 @@ int ctd_batch_run(ctd_ctx *ctx, const ctd_job *jobs, uint32_t njobs, uint32_t *c
             h.add(g.hi);
             h.add(g.first);
             h.add(g.count);
+            h.add(g.gcount);
             h.add(g.any_classified);
         }
         if (!bc.exec || bc.key != h.h) {
             cudaGraph_t graph = nullptr;
             CTX_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            const uint64_t l0 = kernel_launch_count();
             int rc = enqueue();
+            bc.graph_launches = kernel_launch_count() - l0;
             cudaError_t e = cudaStreamEndCapture(st, &graph);
             if (rc) {
                 if (graph)
@@ -428,6 +452,7 @@ int ctd_batch_run(ctd_ctx *ctx, const ctd_job *jobs, uint32_t njobs, uint32_t *c
             bc.key = h.h;
         } else {
             ++bc.replays;
+            note_kernel_launches(bc.graph_launches);  // the kernels the replay runs
         }
         CTX_TRY(cudaGraphLaunch(bc.exec, st));
     }
@@ -752,10 +777,10 @@ int ctd_serve_tick(ctd_server *srv, uint64_t *done_ids, uint32_t cap, uint32_t *
             bool any_cls = false;
             const uint32_t first = used;
             std::vector<uint32_t> ks = kv.second;
-            std::stable_sort(ks.begin(), ks.end(), [&](uint32_t x, uint32_t y) {
-                const ctd_job &a = srv->running[x].job, &c = srv->running[y].job;
-                return (double)(a.n1 - a.n0) * term_cost(a.family) > (double)(c.n1 - c.n0) * term_cost(c.family);
-            });
+            uint32_t gcount[BATCH_GROUPS];
+            order_active(
+                ks, gcount, [&](uint32_t x) { return srv->running[x].job.n1 - srv->running[x].job.n0; },
+                [&](uint32_t x) { return srv->running[x].job.family; });
             for (uint32_t k : ks) {
                 ctd_server::Job &j = srv->running[k];
                 lo = std::min(lo, j.cursor);
@@ -777,7 +802,7 @@ int ctd_serve_tick(ctd_server *srv, uint64_t *done_ids, uint32_t cap, uint32_t *
                 bs.items = srv->d_items;
                 bs.bucket_count = srv->d_bucket;
                 bs.bucket_base = srv->d_bucket + 2ull * (used - first) * CLASS_BUCKETS;
-                rc = launch_batch(srv->d_jobs, d_act + first, used - first, any_cls, srv->d_primes, d_count, lo, hi,
+                rc = launch_batch(srv->d_jobs, d_act + first, gcount, any_cls, srv->d_primes, d_count, lo, hi,
                                   bs, ctx_sm_count(ctx), st, err);
             }
             if (rc)

@@ -38,6 +38,11 @@ struct ctd_ctx {
     // per-family launch and tiling parameters (ctd_set_tuning / ctd_autotune)
     ctd_tuning tuning[10] = {};
     bool tuned[10] = {};
+    // per family and prime width (bit length of the primes, 0..64): what
+    // ctd_autotune measured or ctd_set_tuning_for set; wins over the family
+    // entry above for primes of that width
+    ctd_tuning wtuning[10][65] = {};
+    bool wtuned[10][65] = {};
 };
 
 namespace {
@@ -116,17 +121,23 @@ constexpr uint32_t DEFAULT_ITEMS_PER_THREAD = 8;
 constexpr uint32_t DEFAULT_MIN_TILE = 4096;
 constexpr uint32_t DEFAULT_SEGMENT_LOG2 = 26;
 
-const ctd_tuning *tuning_of(const ctd_ctx *ctx, uint32_t family)
+int bit_length(uint64_t x) { return x ? 64 - __builtin_clzll(x) : 0; }
+
+// the entry in force for `family` at primes of `bits` bits: the width entry,
+// else the family entry, else none (defaults)
+const ctd_tuning *tuning_of(const ctd_ctx *ctx, uint32_t family, int bits)
 {
     const int k = tuning_slot(family);
+    if (bits >= 0 && bits <= 64 && ctx->wtuned[k][bits])
+        return &ctx->wtuning[k][bits];
     return ctx->tuned[k] ? &ctx->tuning[k] : nullptr;
 }
 
-int default_block(const ctd_ctx *ctx, uint32_t family)
+int default_block(const ctd_ctx *ctx, uint32_t family, int bits)
 {
     if (ctx->block_override > 0)
         return ctx->block_override;
-    const ctd_tuning *t = tuning_of(ctx, family);
+    const ctd_tuning *t = tuning_of(ctx, family, bits);
     return t && t->block_size > 0 ? t->block_size : 256;
 }
 
@@ -142,14 +153,14 @@ int grid_for(const ctd_ctx *ctx, uint32_t family, int block, int ctas_per_sm)
     return ctx->sm_count * per_sm;
 }
 
-int default_grid(ctd_ctx *ctx, uint32_t family, int block)
+int default_grid(ctd_ctx *ctx, uint32_t family, int block, int bits)
 {
     if (ctx->grid_override > 0)
         return ctx->grid_override;
     // persistent grid: exactly the CTAs that are resident at once, so every
     // thread strides over the same number of work items and no CTA waits
     // for a second wave
-    const ctd_tuning *t = tuning_of(ctx, family);
+    const ctd_tuning *t = tuning_of(ctx, family, bits);
     return grid_for(ctx, family, block, t ? t->ctas_per_sm : 0);
 }
 
@@ -174,29 +185,29 @@ void tiles_for(uint64_t nprimes, uint64_t N, int grid, int block, uint32_t items
     tiles = (uint32_t)((N + tile_len - 1) / tile_len);
 }
 
-void choose_tiles(const ctd_ctx *ctx, uint32_t family, uint64_t nprimes, uint64_t N, int grid, int block,
+void choose_tiles(const ctd_ctx *ctx, uint32_t family, int bits, uint64_t nprimes, uint64_t N, int grid, int block,
                   uint32_t &tiles, uint64_t &tile_len)
 {
-    const ctd_tuning *t = tuning_of(ctx, family);
+    const ctd_tuning *t = tuning_of(ctx, family, bits);
     tiles_for(nprimes, N, grid, block, t && t->items_per_thread ? t->items_per_thread : DEFAULT_ITEMS_PER_THREAD,
               t && t->min_tile ? t->min_tile : DEFAULT_MIN_TILE, tiles, tile_len);
 }
 
-uint32_t variant_of(const ctd_ctx *ctx, uint32_t family)
+uint32_t variant_of(const ctd_ctx *ctx, uint32_t family, int bits)
 {
-    const ctd_tuning *t = tuning_of(ctx, family);
+    const ctd_tuning *t = tuning_of(ctx, family, bits);
     return t ? t->variant : CTD_VARIANT_AUTO;
 }
 
-uint32_t classify_min_of(const ctd_ctx *ctx, uint32_t family)
+uint32_t classify_min_of(const ctd_ctx *ctx, uint32_t family, int bits)
 {
-    const ctd_tuning *t = tuning_of(ctx, family);
+    const ctd_tuning *t = tuning_of(ctx, family, bits);
     return t && t->classify_min ? t->classify_min : DEFAULT_CLASSIFY_MIN;
 }
 
-uint64_t default_segment(const ctd_ctx *ctx, uint32_t family)
+uint64_t default_segment(const ctd_ctx *ctx, uint32_t family, int bits)
 {
-    const ctd_tuning *t = tuning_of(ctx, family);
+    const ctd_tuning *t = tuning_of(ctx, family, bits);
     return 1ull << (t && t->segment_log2 ? t->segment_log2 : DEFAULT_SEGMENT_LOG2);
 }
 
@@ -223,10 +234,10 @@ int ctx_sm_count(const ctd_ctx *ctx) { return ctx->sm_count; }
 cudaStream_t ctx_stream(const ctd_ctx *ctx) { return ctx->stream; }
 SieveWorkspace *ctx_workspace(const ctd_ctx *ctx) { return ctx->ws; }
 BatchCache *&ctx_batch_cache(ctd_ctx *ctx) { return ctx->batch; }
-ctd_tuning ctx_tuning(ctd_ctx *ctx, uint32_t family)
+ctd_tuning ctx_tuning(ctd_ctx *ctx, uint32_t family, uint64_t first_prime)
 {
     ctd_tuning t{};
-    ctd_get_tuning(ctx, family, &t);
+    ctd_get_tuning_for(ctx, family, (uint32_t)bit_length(first_prime < 3 ? 3 : first_prime), &t);
     return t;
 }
 int ctx_fail(ctd_ctx *ctx, int code, const std::string &msg) { return fail(ctx, code, msg); }
@@ -349,11 +360,13 @@ int ctd_set_launch(ctd_ctx *ctx, int grid_size, int block_size)
 
 int ctd_check_job(const ctd_job *job) { return job_ok(job) ? CTD_OK : CTD_ERR_INVALID_ARGUMENT; }
 
-int ctd_get_tuning(ctd_ctx *ctx, uint32_t family, ctd_tuning *out)
+int ctd_get_tuning(ctd_ctx *ctx, uint32_t family, ctd_tuning *out) { return ctd_get_tuning_for(ctx, family, 0, out); }
+
+int ctd_get_tuning_for(ctd_ctx *ctx, uint32_t family, uint32_t prime_bits, ctd_tuning *out)
 {
-    if (!ctx || !out)
+    if (!ctx || !out || prime_bits > 64)
         return CTD_ERR_INVALID_ARGUMENT;
-    const ctd_tuning *t = tuning_of(ctx, family);
+    const ctd_tuning *t = tuning_of(ctx, family, prime_bits ? (int)prime_bits : -1);
     if (t) {
         *out = *t;
         return CTD_OK;
@@ -367,13 +380,18 @@ int ctd_get_tuning(ctd_ctx *ctx, uint32_t family, ctd_tuning *out)
     return CTD_OK;
 }
 
-int ctd_set_tuning(ctd_ctx *ctx, uint32_t family, const ctd_tuning *t)
+int ctd_set_tuning(ctd_ctx *ctx, uint32_t family, const ctd_tuning *t) { return ctd_set_tuning_for(ctx, family, 0, t); }
+
+int ctd_set_tuning_for(ctd_ctx *ctx, uint32_t family, uint32_t prime_bits, const ctd_tuning *t)
 {
-    if (!ctx)
+    if (!ctx || prime_bits > 64)
         return CTD_ERR_INVALID_ARGUMENT;
     const int k = tuning_slot(family);
     if (!t) {
-        ctx->tuned[k] = false;
+        if (prime_bits)
+            ctx->wtuned[k][prime_bits] = false;
+        else
+            ctx->tuned[k] = false;
         return CTD_OK;
     }
     if (t->block_size < 32 || t->block_size > 256 || (t->block_size % 32) || t->ctas_per_sm < 0 ||
@@ -382,8 +400,13 @@ int ctd_set_tuning(ctd_ctx *ctx, uint32_t family, const ctd_tuning *t)
         return fail(ctx, CTD_ERR_INVALID_ARGUMENT,
                     "ctd_set_tuning: block_size 32..256 (multiple of 32), ctas_per_sm >= 0, items_per_thread and "
                     "min_tile > 0, segment_log2 0 or 20..40, variant 0..2");
-    ctx->tuning[k] = *t;
-    ctx->tuned[k] = true;
+    if (prime_bits) {
+        ctx->wtuning[k][prime_bits] = *t;
+        ctx->wtuned[k][prime_bits] = true;
+    } else {
+        ctx->tuning[k] = *t;
+        ctx->tuned[k] = true;
+    }
     return CTD_OK;
 }
 
@@ -395,10 +418,12 @@ int ctd_autotune(ctd_ctx *ctx, const ctd_job *job, double budget_s, ctd_tuning *
     cudaStream_t st = ctx->stream;
     const auto t0 = std::chrono::steady_clock::now();
     auto elapsed = [&] { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); };
-    ctd_tuning cur{};
-    ctd_get_tuning(ctx, job->family, &cur);
-    // sample: the job's first prime segment (odd primes only)
+    // the sample: the job's first prime segment (odd primes only); the
+    // result is kept for the family at this prime width
     const uint64_t fx = job->f0 < 3 ? 3 : job->f0;
+    const int bits = bit_length(fx);
+    ctd_tuning cur{};
+    ctd_get_tuning_for(ctx, job->family, (uint32_t)bits, &cur);
     const uint64_t seg = 1ull << (cur.segment_log2 ? cur.segment_log2 : DEFAULT_SEGMENT_LOG2);
     const uint64_t fy = job->f1 - fx > seg ? fx + seg : job->f1;
     if (fx >= fy) {
@@ -451,6 +476,15 @@ int ctd_autotune(ctd_ctx *ctx, const ctd_job *job, double budget_s, ctd_tuning *
         }
         return CTD_OK;
     };
+    auto try_config = [&](const ctd_tuning &t, ctd_tuning &winner, float &best_ms) -> int {
+        float ms = 0;
+        const int e = time_config(t, np, ms);
+        if (!e && ms < best_ms) {
+            best_ms = ms;
+            winner = t;
+        }
+        return e;
+    };
     ctd_tuning base = cur;
     base.block_size = 256;
     base.ctas_per_sm = 0;
@@ -466,30 +500,38 @@ int ctd_autotune(ctd_ctx *ctx, const ctd_job *job, double budget_s, ctd_tuning *
         rc = time_config(base, np, best_ms);
     }
     ctd_tuning winner = base;
+    const uint32_t fam = job->family;
+    // power-residue classes (doubling families): always, or never
+    if (!rc && (fam == CTD_PROTH || fam == CTD_RIESEL || fam == CTD_MERSENNE)) {
+        for (uint32_t cm : {1u, 0xffffffffu}) {
+            if (elapsed() >= budget_s)
+                break;
+            ctd_tuning t = winner;
+            t.classify_min = cm;
+            rc = try_config(t, winner, best_ms);
+            if (rc)
+                break;
+        }
+    }
     // launch shape: block size and resident CTAs per SM
     const int blocks[] = {256, 128, 64};
     for (int bi = 0; !rc && bi < 3 && elapsed() < budget_s; ++bi) {
-        const int occ = residue_blocks_per_sm(job->family, blocks[bi]);
+        const int occ = residue_blocks_per_sm(fam, blocks[bi]);
         const int cands[] = {occ, occ - 1, occ / 2, (occ * 3) / 4};
         for (int ci = 0; !rc && ci < 4 && elapsed() < budget_s; ++ci) {
             const int c = cands[ci];
             if (c < 1 || (blocks[bi] == 256 && c == occ))
                 continue;
-            ctd_tuning t = base;
+            ctd_tuning t = winner;
             t.block_size = blocks[bi];
             t.ctas_per_sm = c;
-            float ms = 0;
-            rc = time_config(t, np, ms);
-            if (!rc && ms < best_ms) {
-                best_ms = ms;
-                winner = t;
-            }
+            rc = try_config(t, winner, best_ms);
         }
     }
     // tiling: only where it changes the split of this sample
     const uint32_t items[] = {2, 4, 8, 16, 32};
     const uint32_t tiles_min[] = {1024, 2048, 4096, 8192, 16384};
-    const int wgrid = grid_for(ctx, job->family, winner.block_size, winner.ctas_per_sm);
+    const int wgrid = grid_for(ctx, fam, winner.block_size, winner.ctas_per_sm);
     uint32_t seen_tiles[32];
     int nseen = 0;
     {
@@ -512,16 +554,10 @@ int ctd_autotune(ctd_ctx *ctx, const ctd_job *job, double budget_s, ctd_tuning *
             if (dup || nseen >= 32)
                 continue;
             seen_tiles[nseen++] = tt;
-            float ms = 0;
-            rc = time_config(t, np, ms);
-            if (!rc && ms < best_ms) {
-                best_ms = ms;
-                winner = t;
-            }
+            rc = try_config(t, winner, best_ms);
         }
     // step form: the term-by-term walk against the blocks (doubling, fixed-n),
     // and the Smarandache step variants
-    const uint32_t fam = job->family;
     const bool has_walk = fam == CTD_PROTH || fam == CTD_RIESEL || fam == CTD_MERSENNE ||
                           fam == CTD_PROTH_FIXED_N || fam == CTD_RIESEL_FIXED_N || fam == CTD_SMARANDACHE;
     for (uint32_t v = CTD_VARIANT_WALK; !rc && has_walk && v <= CTD_VARIANT_MONTGOMERY && elapsed() < budget_s; ++v) {
@@ -529,20 +565,55 @@ int ctd_autotune(ctd_ctx *ctx, const ctd_job *job, double budget_s, ctd_tuning *
             break;
         ctd_tuning t = winner;
         t.variant = v;
-        float ms = 0;
-        rc = time_config(t, np, ms);
-        if (!rc && ms < best_ms) {
-            best_ms = ms;
-            winner = t;
+        rc = try_config(t, winner, best_ms);
+    }
+    // segment length: one whole segment (device sieve + residue launch) per
+    // candidate, compared per prime; the plain path walks the job in segments
+    // of the winner's length
+    if (!rc && elapsed() < budget_s) {
+        double best_per_prime = 0;
+        uint32_t best_log2 = winner.segment_log2 ? winner.segment_log2 : DEFAULT_SEGMENT_LOG2;
+        for (uint32_t lg : {26u, 28u, 30u}) {
+            if (elapsed() >= budget_s)
+                break;
+            const uint64_t sy = job->f1 - fx > (1ull << lg) ? fx + (1ull << lg) : job->f1;
+            if (ensure_buffer(ctx, ctx->d_primes, ctx->primes_cap, prime_count_upper_bound(fx, sy)))
+                break;
+            const int grid = grid_for(ctx, fam, winner.block_size, winner.ctas_per_sm);
+            view.variant = winner.variant;
+            view.classify_min = winner.classify_min ? winner.classify_min : DEFAULT_CLASSIFY_MIN;
+            uint64_t n = 0;
+            float t = 0;
+            if (cudaMemsetAsync(ctx->d_counts, 0, N * sizeof(uint32_t), st) != cudaSuccess)
+                break;
+            cudaEventRecord(ea, st);
+            rc = sieve_range(ctx->ws, fx, sy, ctx->d_primes, ctx->primes_cap, &n, st, err);
+            if (!rc && n) {
+                tiles_for(n, N, grid, winner.block_size, winner.items_per_thread, winner.min_tile, view.tiles,
+                          view.tile_len);
+                rc = launch_residues(view, ctx->d_primes, n, grid, winner.block_size, st, err, ctx->rs);
+            }
+            cudaEventRecord(eb, st);
+            if (rc || cudaEventSynchronize(eb) != cudaSuccess)
+                break;
+            cudaEventElapsedTime(&t, ea, eb);
+            const double per_prime = n ? t / (double)n : 1e30;
+            if (!best_per_prime || per_prime < best_per_prime) {
+                best_per_prime = per_prime;
+                best_log2 = lg;
+            }
+            if (sy == job->f1)
+                break;  // the job has no longer segment to offer
         }
+        winner.segment_log2 = best_log2;
     }
     cudaEventDestroy(ea);
     cudaEventDestroy(eb);
     if (rc)
         return fail(ctx, rc, err.empty() ? std::string("ctd_autotune: CUDA error") : err);
-    const int k = tuning_slot(job->family);
-    ctx->tuning[k] = winner;
-    ctx->tuned[k] = true;
+    const int k = tuning_slot(fam);
+    ctx->wtuning[k][bits] = winner;
+    ctx->wtuned[k][bits] = true;
     *best = winner;
     return CTD_OK;
 }
@@ -593,12 +664,15 @@ int ctd_residues_device(ctd_ctx *ctx, const ctd_job *job, const uint64_t *d_prim
         return fail(ctx, CTD_ERR_INVALID_ARGUMENT, "ctd_residues_device: bad arguments");
     CTX_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    // the width of the list's primes: the job's prime range start (the
+    // list holds primes of [f0, f1))
+    const int bits = bit_length(job->f0 < 3 ? 3 : job->f0);
     JobView v = make_view(job, d_counts, d_factors);
-    v.variant = variant_of(ctx, job->family);
-    v.classify_min = classify_min_of(ctx, job->family);
-    const int block = default_block(ctx, job->family);
-    const int grid = default_grid(ctx, job->family, block);
-    choose_tiles(ctx, job->family, nprimes, job->n1 - job->n0, grid, block, v.tiles, v.tile_len);
+    v.variant = variant_of(ctx, job->family, bits);
+    v.classify_min = classify_min_of(ctx, job->family, bits);
+    const int block = default_block(ctx, job->family, bits);
+    const int grid = default_grid(ctx, job->family, block, bits);
+    choose_tiles(ctx, job->family, bits, nprimes, job->n1 - job->n0, grid, block, v.tiles, v.tile_len);
     std::string err;
     int rc = launch_residues(v, d_primes, nprimes, grid, block, st, err, ctx->rs);
     return rc ? fail(ctx, rc, err) : CTD_OK;
@@ -640,8 +714,6 @@ int ctd_run_plain(ctd_ctx *ctx, const ctd_job *job, uint32_t *counts_inout, uint
     CTX_CUDA(cudaMemcpyAsync(ctx->d_counts, counts_inout, N * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
     CTX_CUDA(cudaMemcpyAsync(ctx->d_factors, factors_inout, NF * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
     JobView view = make_view(job, ctx->d_counts, ctx->d_factors);
-    view.variant = variant_of(ctx, job->family);
-    view.classify_min = classify_min_of(ctx, job->family);
     std::string err;
 
     uint64_t f0 = resume_after_prime ? resume_after_prime + 1 : job->f0;
@@ -652,9 +724,9 @@ int ctd_run_plain(ctd_ctx *ctx, const ctd_job *job, uint32_t *counts_inout, uint
         if (rc)
             return fail(ctx, rc, err);
     }
-    const uint64_t seg = segment_length ? segment_length : default_segment(ctx, job->family);
-    const int block = default_block(ctx, job->family);
-    const int grid = default_grid(ctx, job->family, block);
+    // tuning by prime width: the job's first prime sets the segment length,
+    // each segment's first prime its launch shape and step forms
+    const uint64_t seg = segment_length ? segment_length : default_segment(ctx, job->family, bit_length(f0));
     uint64_t last_prime = resume_after_prime;
     uint64_t primes_done = 0;
     for (uint64_t fx = f0, fy = (f1 - f0 > seg) ? f0 + seg : f1; fx < f1;
@@ -670,7 +742,12 @@ int ctd_run_plain(ctd_ctx *ctx, const ctd_job *job, uint32_t *counts_inout, uint
         if (np > ctx->primes_cap)
             return fail(ctx, CTD_ERR_CAPACITY, "prime count above its bound");
         if (np) {
-            choose_tiles(ctx, job->family, np, N, grid, block, view.tiles, view.tile_len);
+            const int bits = bit_length(fx);
+            const int block = default_block(ctx, job->family, bits);
+            const int grid = default_grid(ctx, job->family, block, bits);
+            view.variant = variant_of(ctx, job->family, bits);
+            view.classify_min = classify_min_of(ctx, job->family, bits);
+            choose_tiles(ctx, job->family, bits, np, N, grid, block, view.tiles, view.tile_len);
             rc = launch_residues(view, ctx->d_primes, np, grid, block, st, err, ctx->rs);
             if (rc)
                 return fail(ctx, rc, err);

@@ -159,10 +159,21 @@ struct BatchSpan {
     uint64_t units;
     uint64_t warp_prefix;
 };
+// Walk groups of a batched segment, by the resources their walks need: the
+// doubling families (target filter in shared memory), Smarandache (the
+// multiply pipe) and the rest.  A segment's active list is group-major.
+constexpr int BATCH_GROUPS = 3;
+constexpr int BATCH_DOUBLING = 0, BATCH_MULTIPLY = 1, BATCH_OTHER = 2;
+inline int batch_group(uint32_t family)
+{
+    return (family == CTD_PROTH || family == CTD_RIESEL || family == CTD_MERSENNE) ? BATCH_DOUBLING
+           : family == CTD_SMARANDACHE                                             ? BATCH_MULTIPLY
+                                                                                   : BATCH_OTHER;
+}
 struct BatchControl {
-    uint64_t nclass;          // (classified job, prime) pairs
-    uint64_t total_warps;     // warp items of the walk
-    unsigned long long next;  // walk work counter
+    uint64_t nclass;                        // (classified job, prime) pairs
+    uint64_t total_warps[BATCH_GROUPS];     // warp items of each group's walk
+    unsigned long long next[BATCH_GROUPS];  // the walks' work counters
 };
 // Device scratch of one batched segment (sized by the caller):
 // spans[nactive + 1], codes/items[class pairs], bucket_count[2 * nactive *
@@ -178,10 +189,11 @@ struct BatchScratch {
 };
 // The kernels of one batched segment over the primes of [lo, hi) in
 // d_primes (count read from *d_count on the device): bounds, classes (when
-// any active job is classified), plan, regroup and one walk launch for all
-// families.  Nothing waits on the host.  Each active job's device cursor
-// moves to the end of its part of [lo, hi).
-int launch_batch(BatchJob *d_jobs, const uint32_t *d_active, uint32_t nactive, bool any_classified,
+// any active job is classified), plan, regroup and one walk launch per walk
+// group present; the active list d_active is group-major with gcount[g]
+// jobs in group g.  Nothing waits on the host.  Each active job's device
+// cursor moves to the end of its part of [lo, hi).
+int launch_batch(BatchJob *d_jobs, const uint32_t *d_active, const uint32_t gcount[BATCH_GROUPS], bool any_classified,
                  const uint64_t *d_primes, const uint64_t *d_count, uint64_t lo, uint64_t hi,
                  const BatchScratch &bs, int sm_count, cudaStream_t stream, std::string &err);
 // Odd primes of [lo, hi) into d_out without waiting on the host; the count
@@ -204,6 +216,8 @@ int launch_mod2(const JobView &view, cudaStream_t stream, std::string &err);
 // Number of kernel launches issued by this process so far (diagnostics).
 uint64_t kernel_launch_count();
 void note_kernel_launch();
+// counts n launches at once (the kernels of a replayed graph)
+void note_kernel_launches(uint64_t n);
 
 // Device buffers and the captured schedule of ctd_batch_run, kept by a
 // context across calls (ctd_batch.cu).
@@ -216,8 +230,9 @@ int ctx_sm_count(const ctd_ctx *ctx);
 cudaStream_t ctx_stream(const ctd_ctx *ctx);
 SieveWorkspace *ctx_workspace(const ctd_ctx *ctx);
 BatchCache *&ctx_batch_cache(ctd_ctx *ctx);
-// the launch/tiling parameters in force for a family (defaults when untuned)
-ctd_tuning ctx_tuning(ctd_ctx *ctx, uint32_t family);
+// the launch/tiling parameters in force for a family at primes of
+// first_prime's width (defaults when untuned)
+ctd_tuning ctx_tuning(ctd_ctx *ctx, uint32_t family, uint64_t first_prime);
 int ctx_fail(ctd_ctx *ctx, int code, const std::string &msg);
 
 }  // namespace ctd

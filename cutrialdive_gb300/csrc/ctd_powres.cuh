@@ -51,10 +51,10 @@ CTD_HD void crt_merge(PowerClass &c, uint32_t j, uint32_t q)
     c.M *= q;
 }
 
-// The classifier's multiplications go through one out-of-line function on
-// the device: inlined, its ~140 Montgomery products made a kernel large
-// enough that warps stalled on instruction fetch (ncu: "no instruction"
-// the top stall).
+// The classifier's fixed chains multiply through one out-of-line function
+// on the device (the two powering loops keep theirs inline): with all ~140
+// Montgomery products inlined the kernel was large enough that warps
+// stalled on instruction fetch (ncu: "no instruction" the top stall).
 #ifdef __CUDA_ARCH__
 __device__ __noinline__ uint64_t powres_mul(uint64_t a, uint64_t b, uint64_t p, uint64_t pinv)
 {
@@ -146,7 +146,7 @@ CTD_HD PowerClass doubling_class(const Mont &m, uint64_t k, bool negate)
     {
         const uint64_t e = p1 - e0;
         for (int b = 63 - clz64(e); b >= 0; --b) {
-            A = mul(A, A);
+            A = m.mul(A, A);  // inline: the hot loops stay small
             if ((e >> b) & 1)
                 A = m.dbl(A);
         }
@@ -156,7 +156,7 @@ CTD_HD PowerClass doubling_class(const Mont &m, uint64_t k, bool negate)
         const uint64_t kr = k < p ? k : k % p;
         const uint64_t ks = m.shoup(kr);
         for (int b = 63 - clz64(e0); b >= 0; --b) {
-            B = mul(B, B);
+            B = m.mul(B, B);
             if ((e0 >> b) & 1)
                 B = shoup_mul(B, kr, ks, p);
         }

@@ -31,6 +31,7 @@ std::atomic<uint64_t> g_launches{0};
 }
 
 void note_kernel_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void note_kernel_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 uint64_t kernel_launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 // ----------------------------------------------------------------- push
@@ -671,15 +672,22 @@ __device__ void run_doubling_class(const JobView &job, uint64_t p, uint32_t M, u
             }
         };
         const uint64_t nb = cnt / BS;
-        if (M <= 2) {
-            // giant step w 2^-32M: one or two 32-bit Montgomery reductions
+        if (M <= 4) {
+            // giant step w 2^-32M: M 32-bit Montgomery reductions (four
+            // multiply-adds each, cheaper than a 64-bit Shoup product up to
+            // M = 4; M is the same for all lanes of a warp)
             const uint32_t plo = (uint32_t)p, phi = (uint32_t)(p >> 32), pinv32 = (uint32_t)m.pinv;
             const uint32_t one = (uint32_t)(p & 1);
             if (M == 1)
                 w = run_blocks(tlo, w, nb, [&](uint64_t x) { return redc32(x, plo, phi, pinv32, one); }, replay);
             else
                 w = run_blocks(tlo, w, nb,
-                               [&](uint64_t x) { return redc32(redc32(x, plo, phi, pinv32, one), plo, phi, pinv32, one); },
+                               [&](uint64_t x) {
+#pragma unroll 1
+                                   for (uint32_t r = 0; r < M; ++r)
+                                       x = redc32(x, plo, phi, pinv32, one);
+                                   return x;
+                               },
                                replay);
         } else {
             const uint64_t G = m.from(square_n(m, HM, 5));  // 2^-32M
@@ -1734,7 +1742,6 @@ __global__ void __launch_bounds__(1024) batch_bounds_kernel(BatchJob *__restrict
         }
         spans[nactive].coff = run;
         ctl->nclass = run;
-        ctl->next = 0;
     }
 }
 
@@ -1767,11 +1774,16 @@ __global__ void __launch_bounds__(256) batch_classify_kernel(const BatchJob *__r
     }
 }
 
+// Per job: class bases (classified jobs), its (prime, tile) units and the
+// exclusive prefix of warp items, restarted at each walk group's first job
+// (the active list is group-major: g0 jobs of group 0, g1 of group 1, the
+// rest of group 2).
 __global__ void __launch_bounds__(1024) batch_plan_kernel(const BatchJob *__restrict__ jobs,
                                                           const uint32_t *__restrict__ active, uint32_t nactive,
                                                           BatchSpan *__restrict__ spans, BatchControl *__restrict__ ctl,
                                                           const uint32_t *__restrict__ bucket_count,
-                                                          uint32_t *__restrict__ bucket_base)
+                                                          uint32_t *__restrict__ bucket_base, uint32_t g0,
+                                                          uint32_t g1)
 {
     for (uint32_t i = threadIdx.x; i < nactive; i += blockDim.x) {
         const BatchJob &j = jobs[active[i]];
@@ -1788,13 +1800,16 @@ __global__ void __launch_bounds__(1024) batch_plan_kernel(const BatchJob *__rest
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        uint64_t run = 0;
-        for (uint32_t i = 0; i < nactive; ++i) {
-            spans[i].warp_prefix = run;
-            run += (spans[i].units + 31) / 32;
+        const uint32_t start[BATCH_GROUPS + 1] = {0, g0, g0 + g1, nactive};
+        for (int g = 0; g < BATCH_GROUPS; ++g) {
+            uint64_t run = 0;
+            for (uint32_t i = start[g]; i < start[g + 1]; ++i) {
+                spans[i].warp_prefix = run;
+                run += (spans[i].units + 31) / 32;
+            }
+            ctl->total_warps[g] = run;
+            ctl->next[g] = 0;
         }
-        spans[nactive].warp_prefix = run;
-        ctl->total_warps = run;
     }
 }
 
@@ -1820,44 +1835,56 @@ __global__ void __launch_bounds__(256) batch_regroup_kernel(const uint32_t *__re
     }
 }
 
-// one (prime, tile) unit of a job of any family
+// one (prime, tile) unit of a job of walk group G
+template <int G>
 __device__ __forceinline__ void batch_unit(const BatchJob &j, uint64_t p, uint32_t code, uint64_t s, uint64_t e)
 {
     const JobView &v = j.view;
-    if (j.classified && p < (1ull << 63)) {
-        switch (v.family) {
-        case PROTH: run_doubling_class<PROTH>(v, p, code >> 16, code & 0xffffu, s, e); return;
-        case RIESEL: run_doubling_class<RIESEL>(v, p, code >> 16, code & 0xffffu, s, e); return;
-        default: run_doubling_class<MERSENNE>(v, p, code >> 16, code & 0xffffu, s, e); return;
+    if (G == BATCH_DOUBLING) {
+        if (j.classified && p < (1ull << 63)) {
+            switch (v.family) {
+            case PROTH: run_doubling_class<PROTH>(v, p, code >> 16, code & 0xffffu, s, e); return;
+            case RIESEL: run_doubling_class<RIESEL>(v, p, code >> 16, code & 0xffffu, s, e); return;
+            default: run_doubling_class<MERSENNE>(v, p, code >> 16, code & 0xffffu, s, e); return;
+            }
         }
-    }
-    switch (v.family) {
-    case MERSENNE: run_item<MERSENNE>(v, p, s, e); break;
-    case PROTH: run_item<PROTH>(v, p, s, e); break;
-    case RIESEL: run_item<RIESEL>(v, p, s, e); break;
-    case SMARANDACHE: run_item<SMARANDACHE>(v, p, s, e); break;
-    case FIBONACCI: run_item<FIBONACCI>(v, p, s, e); break;
-    case LUCAS: run_item<LUCAS>(v, p, s, e); break;
-    case PROTH_FIXED_N: run_item<PROTH_FIXED_N>(v, p, s, e); break;
-    case RIESEL_FIXED_N: run_item<RIESEL_FIXED_N>(v, p, s, e); break;
-    case TRIBONACCI: run_item<TRIBONACCI>(v, p, s, e); break;
-    default: run_item<PEANO>(v, p, s, e); break;
+        switch (v.family) {
+        case PROTH: run_item<PROTH>(v, p, s, e); return;
+        case RIESEL: run_item<RIESEL>(v, p, s, e); return;
+        default: run_item<MERSENNE>(v, p, s, e); return;
+        }
+    } else if (G == BATCH_MULTIPLY) {
+        run_item<SMARANDACHE>(v, p, s, e);
+    } else {
+        switch (v.family) {
+        case FIBONACCI: run_item<FIBONACCI>(v, p, s, e); break;
+        case LUCAS: run_item<LUCAS>(v, p, s, e); break;
+        case PROTH_FIXED_N: run_item<PROTH_FIXED_N>(v, p, s, e); break;
+        case RIESEL_FIXED_N: run_item<RIESEL_FIXED_N>(v, p, s, e); break;
+        case TRIBONACCI: run_item<TRIBONACCI>(v, p, s, e); break;
+        default: run_item<PEANO>(v, p, s, e); break;
+        }
     }
 }
 
-constexpr int BATCH_CTAS_PER_SM = 3;  // the target filter's 64 KiB per CTA and 80 registers a thread
+// resident CTAs of a group's walk: the doubling walks keep the target
+// filter's 64 KiB per CTA and 80 registers a thread; the others fit four
+constexpr int batch_ctas_per_sm(int g) { return g == BATCH_DOUBLING ? 3 : 4; }
 
-__global__ void __launch_bounds__(256, BATCH_CTAS_PER_SM)
+// The walk of one group: a persistent grid taking one warp item (32 units
+// of one job: same family, same class) at a time from the group's counter.
+template <int G>
+__global__ void __launch_bounds__(256, batch_ctas_per_sm(G))
 batch_walk_kernel(const BatchJob *__restrict__ jobs, const uint32_t *__restrict__ active, uint32_t nactive,
                   const uint64_t *__restrict__ primes, const BatchSpan *__restrict__ spans,
                   BatchControl *__restrict__ ctl, const ClassItem *__restrict__ items)
 {
-    const uint64_t total = ctl->total_warps;
+    const uint64_t total = ctl->total_warps[G];
     const uint32_t lane = threadIdx.x & 31u;
     for (;;) {
         unsigned long long w = 0;
         if (lane == 0)
-            w = atomicAdd(&ctl->next, 1ull);
+            w = atomicAdd(&ctl->next[G], 1ull);
         w = __shfl_sync(0xffffffffu, w, 0);
         if (w >= total)
             break;
@@ -1872,7 +1899,7 @@ batch_walk_kernel(const BatchJob *__restrict__ jobs, const uint32_t *__restrict_
             const uint64_t e = s + j.view.tile_len < j.view.n1 ? s + j.view.tile_len : j.view.n1;
             uint64_t p;
             uint32_t code = 0;
-            if (j.classified) {
+            if (G == BATCH_DOUBLING && j.classified) {
                 const ClassItem it = items[spans[i].coff + idx];
                 p = it.p;
                 code = it.code;
@@ -1880,15 +1907,35 @@ batch_walk_kernel(const BatchJob *__restrict__ jobs, const uint32_t *__restrict_
                 p = primes[spans[i].pbeg + idx];
             }
             if (s < e)
-                batch_unit(j, p, code, s, e);
+                batch_unit<G>(j, p, code, s, e);
         }
     }
 }
 
-int launch_batch(BatchJob *d_jobs, const uint32_t *d_active, uint32_t nactive, bool any_classified,
+template <int G>
+static cudaError_t launch_walk(const BatchJob *jobs, const uint32_t *active, uint32_t n, const uint64_t *primes,
+                               const BatchSpan *spans, BatchControl *ctl, const ClassItem *items, int sm_count,
+                               cudaStream_t st)
+{
+    const size_t sm = G == BATCH_DOUBLING ? (size_t)FILTER_WORDS * sizeof(uint32_t) * 256 : 0;
+    cudaError_t rc = allow_smem(batch_walk_kernel<G>, sm);
+    int occ = 0;
+    if (rc == cudaSuccess)
+        rc = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_walk_kernel<G>, 256, sm);
+    if (rc == cudaSuccess) {
+        batch_walk_kernel<G><<<sm_count * (occ > 0 ? occ : 1), 256, sm, st>>>(jobs, active, n, primes, spans, ctl,
+                                                                              items);
+        rc = cudaGetLastError();
+        note_kernel_launch();
+    }
+    return rc;
+}
+
+int launch_batch(BatchJob *d_jobs, const uint32_t *d_active, const uint32_t gcount[BATCH_GROUPS], bool any_classified,
                  const uint64_t *d_primes, const uint64_t *d_count, uint64_t lo, uint64_t hi,
                  const BatchScratch &bs, int sm_count, cudaStream_t st, std::string &err)
 {
+    const uint32_t nactive = gcount[0] + gcount[1] + gcount[2];
     if (!nactive)
         return CTD_OK;
     cudaError_t rc = cudaSuccess;
@@ -1909,7 +1956,7 @@ int launch_batch(BatchJob *d_jobs, const uint32_t *d_active, uint32_t nactive, b
     }
     if (rc == cudaSuccess) {
         batch_plan_kernel<<<1, 1024, 0, st>>>(d_jobs, d_active, nactive, bs.spans, bs.ctl, bs.bucket_count,
-                                              bs.bucket_base);
+                                              bs.bucket_base, gcount[0], gcount[1]);
         rc = cudaGetLastError();
         note_kernel_launch();
     }
@@ -1921,19 +1968,17 @@ int launch_batch(BatchJob *d_jobs, const uint32_t *d_active, uint32_t nactive, b
         rc = cudaGetLastError();
         note_kernel_launch();
     }
-    if (rc == cudaSuccess) {
-        const size_t sm = (size_t)FILTER_WORDS * sizeof(uint32_t) * 256;
-        rc = allow_smem(batch_walk_kernel, sm);
-        int occ = 0;
-        if (rc == cudaSuccess)
-            rc = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_walk_kernel, 256, sm);
-        if (rc == cudaSuccess) {
-            batch_walk_kernel<<<sm_count * (occ > 0 ? occ : 1), 256, sm, st>>>(d_jobs, d_active, nactive, d_primes,
-                                                                              bs.spans, bs.ctl, bs.items);
-            rc = cudaGetLastError();
-            note_kernel_launch();
-        }
-    }
+    // the walks, one launch per group present (heaviest work per term first)
+    const uint32_t f1 = gcount[0], f2 = gcount[0] + gcount[1];
+    if (rc == cudaSuccess && gcount[BATCH_MULTIPLY])
+        rc = launch_walk<BATCH_MULTIPLY>(d_jobs, d_active + f1, gcount[1], d_primes, bs.spans + f1, bs.ctl, bs.items,
+                                         sm_count, st);
+    if (rc == cudaSuccess && gcount[BATCH_OTHER])
+        rc = launch_walk<BATCH_OTHER>(d_jobs, d_active + f2, gcount[2], d_primes, bs.spans + f2, bs.ctl, bs.items,
+                                      sm_count, st);
+    if (rc == cudaSuccess && gcount[BATCH_DOUBLING])
+        rc = launch_walk<BATCH_DOUBLING>(d_jobs, d_active, gcount[0], d_primes, bs.spans, bs.ctl, bs.items, sm_count,
+                                         st);
     if (rc != cudaSuccess) {
         err = std::string("batched residue launch: ") + cudaGetErrorString(rc);
         return CTD_ERR_CUDA;

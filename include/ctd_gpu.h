@@ -131,12 +131,23 @@ typedef struct ctd_tuning {
 
 /* The parameters in force for `family` (defaults until tuned or set). */
 int ctd_get_tuning(ctd_ctx *ctx, uint32_t family, ctd_tuning *out);
-/* Sets them; NULL restores the defaults.  ctd_set_launch overrides still win. */
+/* Sets them for every prime width; NULL restores the defaults.
+ * ctd_set_launch overrides still win. */
 int ctd_set_tuning(ctd_ctx *ctx, uint32_t family, const ctd_tuning *t);
-/* Autotuner: times candidate launch shapes, tilings and step forms of the job's family on
- * the job's own first prime segment (its index range, a sample of its primes)
- * for about `budget_s` seconds, applies the fastest to the context and returns
- * it in *best.  Results never depend on the tuning, only the speed. */
+/* The same keyed by prime width: the parameters in force for primes of
+ * `prime_bits` bits (1..64; 0 = the family entry).  A width entry wins over
+ * the family entry for segments whose first prime has that width; NULL
+ * clears it. */
+int ctd_get_tuning_for(ctd_ctx *ctx, uint32_t family, uint32_t prime_bits, ctd_tuning *out);
+int ctd_set_tuning_for(ctd_ctx *ctx, uint32_t family, uint32_t prime_bits, const ctd_tuning *t);
+/* Autotuner: times candidate launch shapes, tilings, step forms, power-residue
+ * classes on or off (doubling families) and the segment length (2^26, 2^28,
+ * 2^30) of the job's family on the job's own first prime segment (its index
+ * range, a sample of its primes) for about `budget_s` seconds, keeps the
+ * fastest in the context for that family at the width of the job's first
+ * prime -- ctd_run_plain, ctd_residues_device, ctd_batch_run and the server
+ * use it there -- and returns it in *best.  Results never depend on the
+ * tuning, only the speed. */
 int ctd_autotune(ctd_ctx *ctx, const ctd_job *job, double budget_s, ctd_tuning *best);
 
 /* Validates a job like the reference's dispatch and range checks

@@ -25,12 +25,17 @@ def test_autotune_keeps_results(eng, case):
     fam, param, n0, n1, f0, f1 = case
     job = ctd.CtdJob(fam, 32, param, n0, n1, f0, f1)
     want = O.trial_factor(fam, param, n0, n1, f0, f1, 32).format()
+    bits = max(3, f0).bit_length()
     try:
         best = eng.autotune(job, budget_s=1.0)
         assert 32 <= best["block_size"] <= 256 and best["block_size"] % 32 == 0
         assert best["ctas_per_sm"] >= 0 and best["items_per_thread"] > 0 and best["min_tile"] > 0
-        assert eng.get_tuning(fam) == best
+        assert best["segment_log2"] in (26, 28, 30)
+        # kept for the family at the width of the job's first prime only
+        assert eng.get_tuning_for(fam, bits) == best
+        assert eng.get_tuning_for(fam, bits + 1) == eng.get_tuning(fam)
         assert run(eng, job) == want
+        eng.set_tuning_for(fam, bits, None)
         # an extreme but valid shape, and every step form: still the same factors
         for variant in (0, 1, 2):
             eng.set_tuning(fam, {"block_size": 64, "ctas_per_sm": 1, "items_per_thread": 32, "min_tile": 1024,
@@ -38,7 +43,27 @@ def test_autotune_keeps_results(eng, case):
             assert run(eng, job) == want, variant
     finally:
         eng.set_tuning(fam, None)
+        eng.set_tuning_for(fam, bits, None)
     assert eng.get_tuning(fam)["segment_log2"] == 26
+
+
+@pytest.mark.parametrize("family,param", [(O.PROTH, 3), (O.MERSENNE, 0), (O.RIESEL, 999_999)])
+def test_classes_on_and_off_same_factors(eng, family, param):
+    """classify_min (the autotuner's power-residue switch) changes only the speed."""
+    n0, n1, f0, f1 = 1, 9001, (1 << 33) - (1 << 21), (1 << 33) + (1 << 21)
+    job = ctd.CtdJob(family, 32, param, n0, n1, f0, f1)
+    outs = []
+    try:
+        for cm in (1, 0xFFFFFFFF):
+            t = eng.get_tuning(family)
+            t["classify_min"] = cm
+            eng.set_tuning_for(family, f0.bit_length(), t)
+            eng.set_tuning_for(family, f1.bit_length(), t)
+            outs.append(run(eng, job))
+    finally:
+        eng.set_tuning_for(family, f0.bit_length(), None)
+        eng.set_tuning_for(family, f1.bit_length(), None)
+    assert outs[0] == outs[1] == O.trial_factor(family, param, n0, n1, f0, f1, 32).format()
 
 
 def test_set_tuning_rejects_bad_values(eng):
