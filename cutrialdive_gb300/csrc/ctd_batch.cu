@@ -487,13 +487,17 @@ int ctd_batch_graph_stats(ctd_ctx *ctx, uint64_t *instantiations, uint64_t *upda
 // ------------------------------------------------------------ the server
 //
 // Slots: the device job table holds max_active entries; a job admitted into
-// a slot keeps it until its results are collected.  Each tick groups the
-// running jobs by the aligned segment their cursor is in (jobs in the same
-// segment share its sieve) and queues, per group, the sieve and one batched
-// launch; the kernels move each job's device cursor to the segment's end.
-// The host keeps the same cursor arithmetic to plan the next tick, so it
-// never reads the device between ticks.  At most TICKS_IN_FLIGHT ticks are
-// queued ahead of the GPU.
+// a slot keeps it until its results are collected.  Each tick advances every
+// running job over one aligned segment of its prime range; the running jobs
+// that are on the same segment share its sieve and its walk launches, and
+// the kernels record each job's progress in its device cursor.  A job's
+// result does not depend on the order of its segments, so an admitted job
+// joins the segment that the most running jobs covering it are on and takes
+// its remaining segments in rotated order (wrapping from its last segment to
+// its first): jobs of overlapping ranges move in step and keep sharing
+// sieves however far apart their arrivals were.  The host plans each tick
+// from its own copy of the segment order, so it never reads the device
+// between ticks.  At most TICKS_IN_FLIGHT ticks are queued ahead of the GPU.
 
 struct ctd_server {
     ctd_ctx *ctx = nullptr;
@@ -505,7 +509,9 @@ struct ctd_server {
         uint32_t slot = 0;
         uint32_t *d_counts = nullptr;
         uint64_t *d_factors = nullptr;
-        uint64_t cursor = 0;  // host mirror of the device cursor
+        // the job's aligned segments seg_first..seg_last, taken in rotated
+        // order from next_seg; segs_left of them remain
+        uint64_t seg_first = 0, seg_last = 0, next_seg = 0, segs_left = 0;
         bool finishing = false;
         cudaEvent_t done_event = nullptr;
         uint32_t *h_counts = nullptr;  // pinned, filled by the final copy
@@ -704,7 +710,23 @@ int ctd_serve_tick(ctd_server *srv, uint64_t *done_ids, uint32_t cap, uint32_t *
             if (rc)
                 return ctx_fail(ctx, rc, err);
         }
-        j.cursor = b.f0;
+        // segments: start where most running jobs covering this one are
+        j.seg_first = b.f0 / srv->seg;
+        j.seg_last = (b.f1 - 1) / srv->seg;
+        j.segs_left = b.f0 < b.f1 ? j.seg_last - j.seg_first + 1 : 0;
+        j.next_seg = j.seg_first;
+        {
+            std::map<uint64_t, uint32_t> votes;
+            for (const ctd_server::Job &r : srv->running)
+                if (r.segs_left && r.next_seg >= j.seg_first && r.next_seg <= j.seg_last)
+                    ++votes[r.next_seg];
+            uint32_t best = 0;
+            for (auto &kv : votes)
+                if (kv.second > best) {
+                    best = kv.second;
+                    j.next_seg = kv.first;
+                }
+        }
         srv->h_stage[j.slot] = b;
         CTX_TRY(cudaMemcpyAsync(srv->d_jobs + j.slot, srv->h_stage + j.slot, sizeof(BatchJob), cudaMemcpyHostToDevice,
                                 st));
@@ -713,13 +735,18 @@ int ctd_serve_tick(ctd_server *srv, uint64_t *done_ids, uint32_t cap, uint32_t *
     if (arc && srv->running.empty())
         return ctx_fail(ctx, arc, err);  // nothing runs and the first queued job cannot be placed
 
-    // 3. one tick: every running job advances over its cursor's segment
+    // 3. one tick: every running job advances over its next segment
     std::map<uint64_t, std::vector<uint32_t>> byseg;  // segment index -> running indices
     for (uint32_t k = 0; k < srv->running.size(); ++k) {
         const ctd_server::Job &j = srv->running[k];
-        if (!j.finishing && j.cursor < j.job.f1)
-            byseg[j.cursor / S].push_back(k);
+        if (!j.finishing && j.segs_left)
+            byseg[j.next_seg].push_back(k);
     }
+    // a job's part of segment k: [max(f0, k S), min(f1, (k + 1) S))
+    auto part_lo = [&](const ctd_server::Job &j, uint64_t k) { return std::max(srv->h_stage[j.slot].f0, k * S); };
+    auto part_hi = [&](const ctd_server::Job &j, uint64_t k) {
+        return k + 1 > ~0ull / S ? j.job.f1 : std::min(j.job.f1, (k + 1) * S);
+    };
     if (!byseg.empty()) {
         // bounded lead over the GPU: wait for the tick before last
         while ((int)srv->inflight.size() >= ctd_server::TICKS_IN_FLIGHT) {
@@ -736,7 +763,7 @@ int ctd_serve_tick(ctd_server *srv, uint64_t *done_ids, uint32_t cap, uint32_t *
                 const ctd_server::Job &j = srv->running[k];
                 maxhi = std::max(maxhi, j.job.f1);
                 if (srv->h_stage[j.slot].classified)
-                    ncls += prime_count_upper_bound(std::max(slo, j.cursor), std::min(slo + S, j.job.f1));
+                    ncls += prime_count_upper_bound(part_lo(j, kv.first), part_hi(j, kv.first));
             }
             class_need = std::max(class_need, ncls);
         }
@@ -772,7 +799,6 @@ int ctd_serve_tick(ctd_server *srv, uint64_t *done_ids, uint32_t cap, uint32_t *
         uint32_t *d_act = srv->d_active + region;
         uint32_t used = 0;
         for (auto &kv : byseg) {
-            const uint64_t slo = kv.first * S;
             uint64_t lo = ~0ull, hi = 0;
             bool any_cls = false;
             const uint32_t first = used;
@@ -783,12 +809,12 @@ int ctd_serve_tick(ctd_server *srv, uint64_t *done_ids, uint32_t cap, uint32_t *
                 [&](uint32_t x) { return srv->running[x].job.family; });
             for (uint32_t k : ks) {
                 ctd_server::Job &j = srv->running[k];
-                lo = std::min(lo, j.cursor);
-                const uint64_t upto = std::min(j.job.f1, slo + S);
-                hi = std::max(hi, upto);
+                lo = std::min(lo, part_lo(j, kv.first));
+                hi = std::max(hi, part_hi(j, kv.first));
                 any_cls |= srv->h_stage[j.slot].classified != 0;
                 h_act[used++] = j.slot;
-                j.cursor = upto;  // the device cursor moves the same way
+                --j.segs_left;
+                j.next_seg = j.next_seg == j.seg_last ? j.seg_first : j.next_seg + 1;
             }
             CTX_TRY(cudaMemcpyAsync(d_act + first, h_act + first, (used - first) * sizeof(uint32_t),
                                     cudaMemcpyHostToDevice, st));
@@ -810,7 +836,7 @@ int ctd_serve_tick(ctd_server *srv, uint64_t *done_ids, uint32_t cap, uint32_t *
         }
         // jobs that reached the end of their range: results to the host
         for (ctd_server::Job &j : srv->running) {
-            if (j.finishing || j.cursor < j.job.f1)
+            if (j.finishing || j.segs_left)
                 continue;
             const uint64_t N = j.job.n1 - j.job.n0;
             CTX_TRY(cudaMallocHost(&j.h_counts, N * sizeof(uint32_t)));

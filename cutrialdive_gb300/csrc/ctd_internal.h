@@ -140,9 +140,10 @@ int launch_residues(const JobView &view, const uint64_t *d_primes, uint64_t npri
 // One job of a batched launch: its view (factors buffer, index range,
 // tiles), its odd-prime range [f0, f1) and whether it walks power-residue
 // classes (doubling families over long ranges).
-// `cursor` is the job's progress on the device: primes below it are done;
-// each segment's bounds kernel starts the job at max(f0, cursor) and moves
-// the cursor to the segment's end.
+// `cursor` is the job's progress on the device: each segment's bounds
+// kernel moves it to the end of the job's part of the segment (the server
+// may take a job's segments in rotated order, see ctd_batch.cu, so it
+// records the last segment done, not a bound below which all are done).
 struct BatchJob {
     JobView view;
     uint64_t f0, f1;

@@ -1719,15 +1719,14 @@ __global__ void __launch_bounds__(1024) batch_bounds_kernel(BatchJob *__restrict
     const uint64_t n = *d_count;
     for (uint32_t i = threadIdx.x; i < nactive; i += blockDim.x) {
         BatchJob &j = jobs[active[i]];
-        // the job's primes of this segment not yet done: [max(f0, cursor, lo), min(f1, hi))
-        uint64_t a = j.f0 > lo ? j.f0 : lo;
-        a = j.cursor > a ? j.cursor : a;
+        // the job's primes of this segment: [max(f0, lo), min(f1, hi))
+        const uint64_t a = j.f0 > lo ? j.f0 : lo;
         const uint64_t b = j.f1 < hi ? j.f1 : hi;
         uint64_t pb = 0, pe = 0;
         if (a < b) {
             pb = lower_bound_u64(primes, n, a);
             pe = lower_bound_u64(primes, n, b);
-            j.cursor = b;  // the walk of this segment completes them
+            j.cursor = b;  // progress: the end of the segment the walk completes
         }
         spans[i].pbeg = pb;
         spans[i].pend = pe;
