@@ -8,9 +8,9 @@
 //   segment ("chunk-major"): each aligned segment is sieved once and
 //   consumed by every job whose range covers it: persistent walk launches
 //   over (job, 32 primes, index tile) work items, one per walk group present
-//   (the doubling families, Smarandache, the rest: each group's kernel has
-//   the occupancy and registers its families need; launch_batch,
-//   ctd_residue.cu).  The whole schedule -- sieves, class and
+//   (doubling over power-residue classes, doubling over every term,
+//   Smarandache, the rest: each group's kernel has the code, occupancy and
+//   registers its families need; launch_batch, ctd_residue.cu).  The whole schedule -- sieves, class and
 //   plan kernels, walks -- is captured once into a CUDA graph; a later call
 //   with the same schedule replays it, one with the same shape updates the
 //   instantiated graph in place, and the device buffers stay with the
@@ -62,16 +62,18 @@ uint64_t odd_f0(const ctd_job &j) { return j.f0 <= 2 ? 3 : j.f0; }
 
 bool is_doubling(uint32_t f) { return f == CTD_PROTH || f == CTD_RIESEL || f == CTD_MERSENNE; }
 
-// Index tiles of a batched job: the longest units a warp item may take.
-// Smarandache terms cost ~11 integer instructions and the walk of each tile
-// starts with an O(log n) jump, so its ranges are cut at 4096 terms;
-// tribonacci at 16384; the rank-of-apparition (Fibonacci, Lucas) and
-// closed-form (fixed-n) paths depend on the whole range and stay whole; the
-// doubling walks are cut at 32768 terms of the full range.
+// Index tiles of a batched job: the longest units a warp item may take, so
+// a long range spreads over many warps.  Each tile starts with the family's
+// O(log n) jump, which for Smarandache costs about a seventh of a
+// 4096-term walk (measured: 4096-term tiles ran the batched Smarandache walk
+// 10 % slower than the untiled per-job kernel), so Smarandache and the
+// doubling walks are cut at 32768 terms and tribonacci at 16384; the
+// rank-of-apparition (Fibonacci, Lucas) and closed-form (fixed-n) paths
+// depend on the whole range and stay whole.
 uint64_t tile_limit(uint32_t family)
 {
     switch (family) {
-    case CTD_SMARANDACHE: return 4096;
+    case CTD_SMARANDACHE: return 32768;
     case CTD_TRIBONACCI: return 16384;
     case CTD_PROTH:
     case CTD_RIESEL:
@@ -226,11 +228,11 @@ struct Segment {
 
 // a segment's active jobs ordered walk group by walk group, heaviest work
 // per prime first within a group (the walks hand out items in this order)
-template <class Terms, class Family>
-void order_active(std::vector<uint32_t> &act, uint32_t gcount[BATCH_GROUPS], Terms terms, Family family)
+template <class Terms, class Family, class Group>
+void order_active(std::vector<uint32_t> &act, uint32_t gcount[BATCH_GROUPS], Terms terms, Family family, Group group)
 {
     std::stable_sort(act.begin(), act.end(), [&](uint32_t x, uint32_t y) {
-        const int gx = batch_group(family(x)), gy = batch_group(family(y));
+        const int gx = group(x), gy = group(y);
         if (gx != gy)
             return gx < gy;
         return (double)terms(x) * term_cost(family(x)) > (double)terms(y) * term_cost(family(y));
@@ -238,7 +240,7 @@ void order_active(std::vector<uint32_t> &act, uint32_t gcount[BATCH_GROUPS], Ter
     for (int g = 0; g < BATCH_GROUPS; ++g)
         gcount[g] = 0;
     for (uint32_t x : act)
-        ++gcount[batch_group(family(x))];
+        ++gcount[group(x)];
 }
 
 // The segments of [lo, hi) aligned to S that some job covers, and their
@@ -283,7 +285,8 @@ Schedule plan_schedule(const std::vector<BatchJob> &hjobs, const ctd_job *jobs, 
             std::vector<uint32_t> slice(act.begin() + b, act.begin() + b + part.count);
             order_active(
                 slice, part.gcount, [&](uint32_t x) { return jobs[x].n1 - jobs[x].n0; },
-                [&](uint32_t x) { return jobs[x].family; });
+                [&](uint32_t x) { return jobs[x].family; },
+                [&](uint32_t x) { return batch_group(jobs[x].family, hjobs[x].classified != 0); });
             part.any_classified = false;
             for (uint32_t x : slice)
                 part.any_classified |= hjobs[x].classified != 0;
@@ -806,7 +809,11 @@ int ctd_serve_tick(ctd_server *srv, uint64_t *done_ids, uint32_t cap, uint32_t *
             uint32_t gcount[BATCH_GROUPS];
             order_active(
                 ks, gcount, [&](uint32_t x) { return srv->running[x].job.n1 - srv->running[x].job.n0; },
-                [&](uint32_t x) { return srv->running[x].job.family; });
+                [&](uint32_t x) { return srv->running[x].job.family; },
+                [&](uint32_t x) {
+                    const ctd_server::Job &j = srv->running[x];
+                    return batch_group(j.job.family, srv->h_stage[j.slot].classified != 0);
+                });
             for (uint32_t k : ks) {
                 ctd_server::Job &j = srv->running[k];
                 lo = std::min(lo, part_lo(j, kv.first));

@@ -160,16 +160,17 @@ struct BatchSpan {
     uint64_t units;
     uint64_t warp_prefix;
 };
-// Walk groups of a batched segment, by the resources their walks need: the
-// doubling families (target filter in shared memory), Smarandache (the
+// Walk groups of a batched segment, by the code and resources their walks
+// need: the doubling families over power-residue classes and over every
+// term (both with the target filter in shared memory), Smarandache (the
 // multiply pipe) and the rest.  A segment's active list is group-major.
-constexpr int BATCH_GROUPS = 3;
-constexpr int BATCH_DOUBLING = 0, BATCH_MULTIPLY = 1, BATCH_OTHER = 2;
-inline int batch_group(uint32_t family)
+constexpr int BATCH_GROUPS = 4;
+constexpr int BATCH_CLASSES = 0, BATCH_DOUBLING = 1, BATCH_MULTIPLY = 2, BATCH_OTHER = 3;
+inline int batch_group(uint32_t family, bool classified)
 {
-    return (family == CTD_PROTH || family == CTD_RIESEL || family == CTD_MERSENNE) ? BATCH_DOUBLING
-           : family == CTD_SMARANDACHE                                             ? BATCH_MULTIPLY
-                                                                                   : BATCH_OTHER;
+    if (family == CTD_PROTH || family == CTD_RIESEL || family == CTD_MERSENNE)
+        return classified ? BATCH_CLASSES : BATCH_DOUBLING;
+    return family == CTD_SMARANDACHE ? BATCH_MULTIPLY : BATCH_OTHER;
 }
 struct BatchControl {
     uint64_t nclass;                        // (classified job, prime) pairs

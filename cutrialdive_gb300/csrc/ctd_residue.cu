@@ -624,8 +624,36 @@ __device__ __forceinline__ uint32_t doubling_class_code(const JobView &job, uint
     return c.M ? (c.M << 16) | c.r : 0u;
 }
 
-// The doubling walk over n = r (mod M) in [s, e), p < 2^63.
-template <uint32_t FAM>
+// The doubling families for p >= 2^63 (beyond the classes' Shoup products):
+// the term-by-term walk of u = k 2^n with carry-safe doubling, out of line so
+// the class walks that call it for such primes keep their registers.
+__device__ __noinline__ void run_doubling_wide(const JobView &job, uint64_t p, uint64_t s, uint64_t e)
+{
+    Mont m;
+    m.init_lite(p);
+    const uint64_t U = m.pow2(s);  // 2^s in Montgomery form
+    uint64_t u;
+    if (job.family == MERSENNE) {
+        u = m.from(U);
+    } else {
+        const uint64_t k = job.param < p ? job.param : job.param % p;
+        u = m.mul(U, k);  // Montgomery form times a plain k: the plain k 2^s mod p
+    }
+    const uint64_t target = job.family == PROTH ? p - 1 : 1;
+    walk_target(u, target, p, s - job.n0, e - s - 1, job.fb, [p](uint64_t x) { return dblmod(x, p); });
+}
+
+// the target of w for the job's doubling family, chosen at run time
+__device__ __forceinline__ uint64_t doubling_target_of(const JobView &job, uint64_t p)
+{
+    return job.family == PROTH    ? doubling_target<PROTH>(job, p)
+           : job.family == RIESEL ? doubling_target<RIESEL>(job, p)
+                                  : doubling_target<MERSENNE>(job, p);
+}
+
+// The doubling walk over n = r (mod M) in [s, e), p < 2^63.  One body for
+// the three families (they differ only in the target), so the kernels that
+// walk classes of several families hold one copy of it.
 __device__ void run_doubling_class(const JobView &job, uint64_t p, uint32_t M, uint32_t r, uint64_t s, uint64_t e)
 {
     const uint32_t sr = (uint32_t)(s % M);
@@ -636,7 +664,7 @@ __device__ void run_doubling_class(const JobView &job, uint64_t p, uint32_t M, u
     const uint64_t cnt = (e - 1 - nf) / M + 1;  // terms nf, nf + M, ... below e
     Mont m;
     m.init(p);
-    const uint64_t wt = doubling_target<FAM>(job, p);
+    const uint64_t wt = doubling_target_of(job, p);
     const uint64_t nr = nf < p - 1 ? nf : nf % (p - 1);
     uint64_t w = m.from(m.pow2(p - 1 - nr));  // 2^-nf (Fermat)
     // 2^-M in Montgomery form: left-to-right powering of 2^-1, each set bit a
@@ -672,22 +700,17 @@ __device__ void run_doubling_class(const JobView &job, uint64_t p, uint32_t M, u
             }
         };
         const uint64_t nb = cnt / BS;
-        if (M <= 4) {
-            // giant step w 2^-32M: M 32-bit Montgomery reductions (four
-            // multiply-adds each, cheaper than a 64-bit Shoup product up to
-            // M = 4; M is the same for all lanes of a warp)
+        if (M <= 2) {
+            // giant step w 2^-32M: one or two 32-bit Montgomery reductions
+            // (a loop of M reductions for M up to 4, measured, ran the walk
+            // 34 % slower than the 64-bit Shoup product for M = 3, 4)
             const uint32_t plo = (uint32_t)p, phi = (uint32_t)(p >> 32), pinv32 = (uint32_t)m.pinv;
             const uint32_t one = (uint32_t)(p & 1);
             if (M == 1)
                 w = run_blocks(tlo, w, nb, [&](uint64_t x) { return redc32(x, plo, phi, pinv32, one); }, replay);
             else
                 w = run_blocks(tlo, w, nb,
-                               [&](uint64_t x) {
-#pragma unroll 1
-                                   for (uint32_t r = 0; r < M; ++r)
-                                       x = redc32(x, plo, phi, pinv32, one);
-                                   return x;
-                               },
+                               [&](uint64_t x) { return redc32(redc32(x, plo, phi, pinv32, one), plo, phi, pinv32, one); },
                                replay);
         } else {
             const uint64_t G = m.from(square_n(m, HM, 5));  // 2^-32M
@@ -1638,9 +1661,9 @@ class_walk_kernel(JobView job, const ClassItem *__restrict__ items, ClassCounter
             const ClassItem it = items[i];
             if (s < e) {
                 if (it.p >= (1ull << 63))
-                    run_doubling<FAM>(job, it.p, s, e);
+                    run_doubling_wide(job, it.p, s, e);
                 else
-                    run_doubling_class<FAM>(job, it.p, it.code >> 16, it.code & 0xffffu, s, e);
+                    run_doubling_class(job, it.p, it.code >> 16, it.code & 0xffffu, s, e);
             }
         }
     }
@@ -1775,14 +1798,15 @@ __global__ void __launch_bounds__(256) batch_classify_kernel(const BatchJob *__r
 
 // Per job: class bases (classified jobs), its (prime, tile) units and the
 // exclusive prefix of warp items, restarted at each walk group's first job
-// (the active list is group-major: g0 jobs of group 0, g1 of group 1, the
-// rest of group 2).
+// (the active list is group-major: g.n[0] jobs of group 0, then group 1 ...).
+struct GroupCounts {
+    uint32_t n[BATCH_GROUPS];
+};
 __global__ void __launch_bounds__(1024) batch_plan_kernel(const BatchJob *__restrict__ jobs,
                                                           const uint32_t *__restrict__ active, uint32_t nactive,
                                                           BatchSpan *__restrict__ spans, BatchControl *__restrict__ ctl,
                                                           const uint32_t *__restrict__ bucket_count,
-                                                          uint32_t *__restrict__ bucket_base, uint32_t g0,
-                                                          uint32_t g1)
+                                                          uint32_t *__restrict__ bucket_base, GroupCounts gc)
 {
     for (uint32_t i = threadIdx.x; i < nactive; i += blockDim.x) {
         const BatchJob &j = jobs[active[i]];
@@ -1799,7 +1823,10 @@ __global__ void __launch_bounds__(1024) batch_plan_kernel(const BatchJob *__rest
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        const uint32_t start[BATCH_GROUPS + 1] = {0, g0, g0 + g1, nactive};
+        uint32_t start[BATCH_GROUPS + 1];
+        start[0] = 0;
+        for (int g = 0; g < BATCH_GROUPS; ++g)
+            start[g + 1] = start[g] + gc.n[g];
         for (int g = 0; g < BATCH_GROUPS; ++g) {
             uint64_t run = 0;
             for (uint32_t i = start[g]; i < start[g + 1]; ++i) {
@@ -1839,14 +1866,12 @@ template <int G>
 __device__ __forceinline__ void batch_unit(const BatchJob &j, uint64_t p, uint32_t code, uint64_t s, uint64_t e)
 {
     const JobView &v = j.view;
-    if (G == BATCH_DOUBLING) {
-        if (j.classified && p < (1ull << 63)) {
-            switch (v.family) {
-            case PROTH: run_doubling_class<PROTH>(v, p, code >> 16, code & 0xffffu, s, e); return;
-            case RIESEL: run_doubling_class<RIESEL>(v, p, code >> 16, code & 0xffffu, s, e); return;
-            default: run_doubling_class<MERSENNE>(v, p, code >> 16, code & 0xffffu, s, e); return;
-            }
-        }
+    if (G == BATCH_CLASSES) {
+        if (p < (1ull << 63))
+            run_doubling_class(v, p, code >> 16, code & 0xffffu, s, e);
+        else
+            run_doubling_wide(v, p, s, e);
+    } else if (G == BATCH_DOUBLING) {
         switch (v.family) {
         case PROTH: run_item<PROTH>(v, p, s, e); return;
         case RIESEL: run_item<RIESEL>(v, p, s, e); return;
@@ -1868,7 +1893,8 @@ __device__ __forceinline__ void batch_unit(const BatchJob &j, uint64_t p, uint32
 
 // resident CTAs of a group's walk: the doubling walks keep the target
 // filter's 64 KiB per CTA and 80 registers a thread; the others fit four
-constexpr int batch_ctas_per_sm(int g) { return g == BATCH_DOUBLING ? 3 : 4; }
+constexpr bool batch_filter(int g) { return g == BATCH_CLASSES || g == BATCH_DOUBLING; }
+constexpr int batch_ctas_per_sm(int g) { return batch_filter(g) ? 3 : 4; }
 
 // The walk of one group: a persistent grid taking one warp item (32 units
 // of one job: same family, same class) at a time from the group's counter.
@@ -1898,7 +1924,7 @@ batch_walk_kernel(const BatchJob *__restrict__ jobs, const uint32_t *__restrict_
             const uint64_t e = s + j.view.tile_len < j.view.n1 ? s + j.view.tile_len : j.view.n1;
             uint64_t p;
             uint32_t code = 0;
-            if (G == BATCH_DOUBLING && j.classified) {
+            if (G == BATCH_CLASSES) {
                 const ClassItem it = items[spans[i].coff + idx];
                 p = it.p;
                 code = it.code;
@@ -1916,7 +1942,7 @@ static cudaError_t launch_walk(const BatchJob *jobs, const uint32_t *active, uin
                                const BatchSpan *spans, BatchControl *ctl, const ClassItem *items, int sm_count,
                                cudaStream_t st)
 {
-    const size_t sm = G == BATCH_DOUBLING ? (size_t)FILTER_WORDS * sizeof(uint32_t) * 256 : 0;
+    const size_t sm = batch_filter(G) ? (size_t)FILTER_WORDS * sizeof(uint32_t) * 256 : 0;
     cudaError_t rc = allow_smem(batch_walk_kernel<G>, sm);
     int occ = 0;
     if (rc == cudaSuccess)
@@ -1934,7 +1960,13 @@ int launch_batch(BatchJob *d_jobs, const uint32_t *d_active, const uint32_t gcou
                  const uint64_t *d_primes, const uint64_t *d_count, uint64_t lo, uint64_t hi,
                  const BatchScratch &bs, int sm_count, cudaStream_t st, std::string &err)
 {
-    const uint32_t nactive = gcount[0] + gcount[1] + gcount[2];
+    GroupCounts gc;
+    uint32_t nactive = 0, first[BATCH_GROUPS];
+    for (int g = 0; g < BATCH_GROUPS; ++g) {
+        gc.n[g] = gcount[g];
+        first[g] = nactive;
+        nactive += gcount[g];
+    }
     if (!nactive)
         return CTD_OK;
     cudaError_t rc = cudaSuccess;
@@ -1955,7 +1987,7 @@ int launch_batch(BatchJob *d_jobs, const uint32_t *d_active, const uint32_t gcou
     }
     if (rc == cudaSuccess) {
         batch_plan_kernel<<<1, 1024, 0, st>>>(d_jobs, d_active, nactive, bs.spans, bs.ctl, bs.bucket_count,
-                                              bs.bucket_base, gcount[0], gcount[1]);
+                                              bs.bucket_base, gc);
         rc = cudaGetLastError();
         note_kernel_launch();
     }
@@ -1968,16 +2000,15 @@ int launch_batch(BatchJob *d_jobs, const uint32_t *d_active, const uint32_t gcou
         note_kernel_launch();
     }
     // the walks, one launch per group present (heaviest work per term first)
-    const uint32_t f1 = gcount[0], f2 = gcount[0] + gcount[1];
-    if (rc == cudaSuccess && gcount[BATCH_MULTIPLY])
-        rc = launch_walk<BATCH_MULTIPLY>(d_jobs, d_active + f1, gcount[1], d_primes, bs.spans + f1, bs.ctl, bs.items,
-                                         sm_count, st);
-    if (rc == cudaSuccess && gcount[BATCH_OTHER])
-        rc = launch_walk<BATCH_OTHER>(d_jobs, d_active + f2, gcount[2], d_primes, bs.spans + f2, bs.ctl, bs.items,
-                                      sm_count, st);
-    if (rc == cudaSuccess && gcount[BATCH_DOUBLING])
-        rc = launch_walk<BATCH_DOUBLING>(d_jobs, d_active, gcount[0], d_primes, bs.spans, bs.ctl, bs.items, sm_count,
-                                         st);
+#define CTD_WALK(G)                                                                                              \
+    if (rc == cudaSuccess && gcount[G])                                                                          \
+        rc = launch_walk<G>(d_jobs, d_active + first[G], gcount[G], d_primes, bs.spans + first[G], bs.ctl, bs.items, \
+                            sm_count, st);
+    CTD_WALK(BATCH_MULTIPLY)
+    CTD_WALK(BATCH_OTHER)
+    CTD_WALK(BATCH_CLASSES)
+    CTD_WALK(BATCH_DOUBLING)
+#undef CTD_WALK
     if (rc != cudaSuccess) {
         err = std::string("batched residue launch: ") + cudaGetErrorString(rc);
         return CTD_ERR_CUDA;
