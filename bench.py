@@ -95,9 +95,9 @@ FAMILY_NAMES = {0: "MERSENNE", 1: "PROTH", 2: "RIESEL", 3: "SMARANDACHE", 4: "FI
 #    shifts per block = 57/18 ALU operations per update, against the ALU
 #    compare rate measured now.
 PROTH_NCU = {"primes": 6047768,
-             "thread_inst": {"classify_kernel": 1522607948 * 23.41, "regroup_kernel": 26304262 * 19.28,
-                             "class_walk_kernel": 3471573154 * 30.47},
-             "dram_bytes": (48.453888 + 0.735232 + 72.707328 + 12.887040 + 55.490304 + 8.239104) * 1e6}
+             "thread_inst": {"classify_kernel": 1704395164 * 23.81, "regroup_kernel": 26304262 * 19.28,
+                             "class_walk_kernel": 3459736685 * 30.50},
+             "dram_bytes": (48.427008 + 0.690176 + 72.707328 + 12.887040 + 55.496192 + 7.038720) * 1e6}
 SMARANDACHE_MULS_PER_UPDATE = 3
 TRIBONACCI_ALU_OPS_PER_UPDATE = 57 / 18
 
