@@ -708,8 +708,9 @@ def measure_served(args, eng, local) -> dict:
         "server": "ctd_serve_* with max_active 256, 2^30 segments per tick, ticks queued up to two ahead",
         "sweep": sweep,
         "identical_to_reference": bool(ref_ok and checked > 0),
-        "reference_check": f"{checked} jobs among the stream's first 200: factor lines with p < 2^a + 2^22 equal "
-                           "the reference engine's files (tests/golden/golden_job_mixes.json)",
+        "reference_check": f"{checked} results of the stream's first 200 jobs, summed over the rates: factor lines "
+                           "with p < 2^a + 2^22 equal the reference engine's files "
+                           "(tests/golden/golden_job_mixes.json)",
         "gpu_launches": int(L.ctd_kernel_launches() - l0),
         "clocks": clocks.summary(),
     }
