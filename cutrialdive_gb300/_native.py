@@ -38,10 +38,10 @@ class CtdProgress(ctypes.Structure):
 
 class CtdTuning(ctypes.Structure):
     _fields_ = [("block_size", i32), ("ctas_per_sm", i32), ("items_per_thread", u32), ("min_tile", u32),
-                ("segment_log2", u32), ("variant", u32), ("classify_min", u32), ("reserved", u32)]
+                ("segment_log2", u32), ("variant", u32), ("classify_min", u32), ("refine_q", u32)]
 
     def as_dict(self) -> dict:
-        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 PROGRESS_CB = ctypes.CFUNCTYPE(i32, vp, ctypes.POINTER(CtdProgress), i32)

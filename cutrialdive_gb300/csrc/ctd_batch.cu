@@ -105,6 +105,7 @@ BatchJob batch_job_of(ctd_ctx *ctx, const ctd_job &j, uint32_t *counts, uint64_t
     v.family = j.family;
     v.variant = t.variant;
     v.classify_min = t.classify_min ? t.classify_min : DEFAULT_CLASSIFY_MIN;
+    v.refine_q = t.refine_q;
     v.param = j.param;
     v.n0 = j.n0;
     v.n1 = j.n1;

@@ -205,6 +205,12 @@ uint32_t classify_min_of(const ctd_ctx *ctx, uint32_t family, int bits)
     return t && t->classify_min ? t->classify_min : DEFAULT_CLASSIFY_MIN;
 }
 
+uint32_t refine_q_of(const ctd_ctx *ctx, uint32_t family, int bits)
+{
+    const ctd_tuning *t = tuning_of(ctx, family, bits);
+    return t ? t->refine_q : 0;
+}
+
 uint64_t default_segment(const ctd_ctx *ctx, uint32_t family, int bits)
 {
     const ctd_tuning *t = tuning_of(ctx, family, bits);
@@ -458,6 +464,7 @@ int ctd_autotune(ctd_ctx *ctx, const ctd_job *job, double budget_s, ctd_tuning *
         tiles_for(n, N, grid, c.block_size, c.items_per_thread, c.min_tile, view.tiles, view.tile_len);
         view.variant = c.variant;
         view.classify_min = c.classify_min ? c.classify_min : DEFAULT_CLASSIFY_MIN;
+        view.refine_q = c.refine_q;
         ms = 1e30f;
         for (int r = 0; r < 3; ++r) {
             if (cudaMemsetAsync(ctx->d_counts, 0, N * sizeof(uint32_t), st) != cudaSuccess)
@@ -501,7 +508,8 @@ int ctd_autotune(ctd_ctx *ctx, const ctd_job *job, double budget_s, ctd_tuning *
     }
     ctd_tuning winner = base;
     const uint32_t fam = job->family;
-    // power-residue classes (doubling families): always, or never
+    // power-residue classes (doubling families): always, or never; then the
+    // rare primes of their refinement: none, up to 31, all (up to 61)
     if (!rc && (fam == CTD_PROTH || fam == CTD_RIESEL || fam == CTD_MERSENNE)) {
         for (uint32_t cm : {1u, 0xffffffffu}) {
             if (elapsed() >= budget_s)
@@ -511,6 +519,13 @@ int ctd_autotune(ctd_ctx *ctx, const ctd_job *job, double budget_s, ctd_tuning *
             rc = try_config(t, winner, best_ms);
             if (rc)
                 break;
+        }
+        for (uint32_t rq : {1u, 31u}) {
+            if (rc || elapsed() >= budget_s || winner.classify_min == 0xffffffffu)
+                break;
+            ctd_tuning t = winner;
+            t.refine_q = rq;
+            rc = try_config(t, winner, best_ms);
         }
     }
     // launch shape: block size and resident CTAs per SM
@@ -582,6 +597,7 @@ int ctd_autotune(ctd_ctx *ctx, const ctd_job *job, double budget_s, ctd_tuning *
             const int grid = grid_for(ctx, fam, winner.block_size, winner.ctas_per_sm);
             view.variant = winner.variant;
             view.classify_min = winner.classify_min ? winner.classify_min : DEFAULT_CLASSIFY_MIN;
+            view.refine_q = winner.refine_q;
             uint64_t n = 0;
             float t = 0;
             if (cudaMemsetAsync(ctx->d_counts, 0, N * sizeof(uint32_t), st) != cudaSuccess)
@@ -670,6 +686,7 @@ int ctd_residues_device(ctd_ctx *ctx, const ctd_job *job, const uint64_t *d_prim
     JobView v = make_view(job, d_counts, d_factors);
     v.variant = variant_of(ctx, job->family, bits);
     v.classify_min = classify_min_of(ctx, job->family, bits);
+    v.refine_q = refine_q_of(ctx, job->family, bits);
     const int block = default_block(ctx, job->family, bits);
     const int grid = default_grid(ctx, job->family, block, bits);
     choose_tiles(ctx, job->family, bits, nprimes, job->n1 - job->n0, grid, block, v.tiles, v.tile_len);
@@ -747,6 +764,7 @@ int ctd_run_plain(ctd_ctx *ctx, const ctd_job *job, uint32_t *counts_inout, uint
             const int grid = default_grid(ctx, job->family, block, bits);
             view.variant = variant_of(ctx, job->family, bits);
             view.classify_min = classify_min_of(ctx, job->family, bits);
+            view.refine_q = refine_q_of(ctx, job->family, bits);
             choose_tiles(ctx, job->family, bits, np, N, grid, block, view.tiles, view.tile_len);
             rc = launch_residues(view, ctx->d_primes, np, grid, block, st, err, ctx->rs);
             if (rc)

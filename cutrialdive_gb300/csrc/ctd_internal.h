@@ -43,6 +43,8 @@ struct JobView {
     uint32_t tiles;      // index tiles per prime (>= 1)
     uint32_t variant;    // step form (CTD_VARIANT_*)
     uint32_t classify_min;  // doubling families: index ranges this long or longer walk power-residue classes
+    uint32_t refine_q;   // largest rare prime whose character refines the classes (0: 61; < 11: none)
+    uint32_t pad;
     uint64_t param;      // k, n or base
     uint64_t n0, n1;     // index range of the factors buffer
     uint64_t tile_len;   // indices per tile (last tile may be shorter)
@@ -104,11 +106,15 @@ int noalloc_prepare(int device, std::string &err);
 // regrouped by class so a warp's lanes walk classes of equal length.  Owned
 // by a context; grown on demand (never during a graph capture).
 // classes: the divisors of 2^3 * 3 * 5 * 7, ranked by size
-constexpr uint32_t CLASS_BUCKETS = 32;
+// classes ranked by M: the 32 divisors of 840, then M above 840 by half
+// octaves (M < 2^16)
+constexpr uint32_t CLASS_BUCKETS = 48;
 struct ClassCounters {
     uint32_t count[CLASS_BUCKETS];  // primes per class
     uint32_t fill[CLASS_BUCKETS];   // regroup cursors
     unsigned long long next;        // walk work counter
+    uint32_t nrefine;               // primes listed for the rare-prime refinement
+    uint32_t pad;
 };
 // a prime with its class code (M << 16 | r)
 struct ClassItem {
@@ -121,6 +127,7 @@ struct ResidueScratch {
     int sm_count = 1;
     uint32_t *codes = nullptr;
     ClassItem *items = nullptr;
+    uint32_t *refine = nullptr;  // indices of the primes to refine
     uint64_t cap = 0;  // primes
     ClassCounters *counters = nullptr;
 };

@@ -117,6 +117,35 @@ CTD_HD Pow105 pow105(const Mont &m, uint64_t x)
     return Pow105{x15, x21, x35, x105};
 }
 
+// A = 2^-e = 2^(p - 1 - e) (left-to-right, a set bit a doubling) and B =
+// wt^e = (-+1)^e k^e (left-to-right, Shoup multiplications by the plain k),
+// both in Montgomery form; 0 < e < p - 1, m with r2.
+CTD_HD void power_pair(const Mont &m, uint64_t k, bool negate, uint64_t e, uint64_t &A, uint64_t &B)
+{
+    const uint64_t p = m.p;
+    A = m.one;
+    {
+        const uint64_t ea = p - 1 - e;
+        for (int b = 63 - clz64(ea); b >= 0; --b) {
+            A = m.mul(A, A);  // inline: the hot loops stay small
+            if ((ea >> b) & 1)
+                A = m.dbl(A);
+        }
+    }
+    B = m.one;
+    {
+        const uint64_t kr = k < p ? k : k % p;
+        const uint64_t ks = m.shoup(kr);
+        for (int b = 63 - clz64(e); b >= 0; --b) {
+            B = m.mul(B, B);
+            if ((e >> b) & 1)
+                B = shoup_mul(B, kr, ks, p);
+        }
+        if (negate && (e & 1))
+            B = B ? p - B : 0;
+    }
+}
+
 // The class of the zeros of 2^-n = wt (mod p), wt = -k (negate) or k, for
 // an odd prime p < 2^63 and a plain k with k mod p != 0; m fully
 // initialised (r2 is needed for k's Shoup quotient).  The work is the same
@@ -139,30 +168,8 @@ CTD_HD PowerClass doubling_class(const Mont &m, uint64_t k, bool negate)
     e0 = f5 ? e0 / 5 : e0;
     e0 = f7 ? e0 / 7 : e0;
     auto mul = [&](uint64_t a, uint64_t b) { return powres_mul(a, b, p, m.pinv); };
-    // A = 2^-e0 = 2^(p - 1 - e0) (left-to-right, a set bit a doubling); B =
-    // wt^e0 = (-+1)^e0 k^e0 by left-to-right powering with Shoup
-    // multiplications by the plain k
-    uint64_t A = m.one;
-    {
-        const uint64_t e = p1 - e0;
-        for (int b = 63 - clz64(e); b >= 0; --b) {
-            A = m.mul(A, A);  // inline: the hot loops stay small
-            if ((e >> b) & 1)
-                A = m.dbl(A);
-        }
-    }
-    uint64_t B = m.one;
-    {
-        const uint64_t kr = k < p ? k : k % p;
-        const uint64_t ks = m.shoup(kr);
-        for (int b = 63 - clz64(e0); b >= 0; --b) {
-            B = m.mul(B, B);
-            if ((e0 >> b) & 1)
-                B = shoup_mul(B, kr, ks, p);
-        }
-        if (negate && (e0 & 1))
-            B = B ? p - B : 0;
-    }
+    uint64_t A, B;
+    power_pair(m, k, negate, e0, A, B);
     // A and B lie in the D-th roots of unity.  For a q that does not divide
     // p - 1 the fixed exponents below map them to 1 (no condition); for one
     // that does, they differ from (p - 1)/q by a factor prime to q, which
@@ -231,6 +238,106 @@ CTD_HD PowerClass doubling_class(const Mont &m, uint64_t k, bool negate)
             return PowerClass{1, 0};
         crt_merge(c, j, q);
     }
+    return c;
+}
+
+// ---- refinement by the character of a rarer prime q = 11 .. 61
+// A prime q divides p - 1 for one prime p in q - 1, and then its character
+// keeps one term in q (or none), so over the classes above the walk shrinks
+// by about prod (1 - 1/q) = 0.58 for q = 11 .. 61.  The refinement costs two
+// more full powers, for the primes that have such a q only: the kernels run
+// it as a separate pass over those primes (a quarter of them), so no warp
+// carries lanes that skip it.  It takes the smallest such q of each prime
+// (the one that shrinks the walk most): one power pair and one discrete
+// logarithm per prime, the same code for every lane whatever its q (taking
+// every q of the primes that have two or more ran the pass twice as long for
+// the extra 1/q of their walks).
+constexpr int POWRES_RARE_COUNT = 14;
+// the rare q, 6 bits each: 11, 13, 17, 19, 23, 29, 31, 37, 41, 43 | 47, 53, 59, 61
+constexpr uint64_t POWRES_RARE_LO = 11ull | 13ull << 6 | 17ull << 12 | 19ull << 18 | 23ull << 24 | 29ull << 30 |
+                                    31ull << 36 | 37ull << 42 | 41ull << 48 | 43ull << 54;
+constexpr uint64_t POWRES_RARE_HI = 47ull | 53ull << 6 | 59ull << 12 | 61ull << 18;
+CTD_HD uint32_t powres_rare_q(int i)
+{
+    return (uint32_t)((i < 10 ? POWRES_RARE_LO >> (6 * i) : POWRES_RARE_HI >> (6 * (i - 10))) & 63u);
+}
+// classes stay below 2^16: the walks' item code packs M and r in 16 bits
+// each (840 * 61 = 51240)
+constexpr uint32_t POWRES_MAX_M = 65535;
+
+// the smallest rare q <= qmax dividing p - 1; 0 when there is none
+CTD_HD uint32_t rare_q_of(uint64_t p, uint32_t qmax)
+{
+    const uint64_t p1 = p - 1;
+    // three 64-bit reductions by products of the q, then 32-bit ones
+    const uint32_t r0 = (uint32_t)(p1 % (11ull * 13 * 17 * 19 * 23 * 29));
+    const uint32_t r1 = (uint32_t)(p1 % (31ull * 37 * 41 * 43 * 47));
+    const uint32_t r2 = (uint32_t)(p1 % (53ull * 59 * 61));
+    uint32_t found = 0;
+#pragma unroll
+    for (int i = POWRES_RARE_COUNT - 1; i >= 0; --i) {
+        const uint32_t q = powres_rare_q(i);
+        const uint32_t r = i < 6 ? r0 : i < 11 ? r1 : r2;
+        found = q <= qmax && r % q == 0 ? q : found;
+    }
+    return found;
+}
+
+// j < q with z^j = y, for z of prime order q, 11 <= q <= 64 (baby steps
+// z^0 .. z^7, giant steps by z^-8 = z^(q - 8)); q when there is none
+CTD_HD uint32_t small_log(const Mont &m, uint64_t z, uint64_t y, uint32_t q)
+{
+    auto mul = [&](uint64_t a, uint64_t b) { return powres_mul(a, b, m.p, m.pinv); };
+    uint64_t baby[8];
+    baby[0] = m.one;
+#pragma unroll
+    for (int j = 1; j < 8; ++j)
+        baby[j] = mul(baby[j - 1], z);
+    const uint64_t g = small_pow(m, z, q - 8);
+    uint64_t t = y;
+    uint32_t found = q;
+    for (uint32_t i = 0; 8 * i < q && found == q; ++i) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (t == baby[j] && 8 * i + j < q && found == q)
+                found = 8 * i + j;
+        t = mul(t, g);
+    }
+    return found;
+}
+
+// n = r (mod M) and n = j (mod q) for a prime q <= 64 not dividing M:
+// n = r + M t with t = (j - r) M^-1 (mod q), the inverse by Fermat
+// (M^(q-2)); 32-bit arithmetic
+CTD_HD void crt_merge_small(PowerClass &c, uint32_t j, uint32_t q)
+{
+    const uint32_t d = c.M % q;
+    uint32_t inv = 1, b = d;
+    for (uint32_t e = q - 2; e; e >>= 1) {
+        if (e & 1)
+            inv = inv * b % q;
+        b = b * b % q;
+    }
+    const uint32_t t = (j + q - c.r % q) % q * inv % q;
+    c.r += c.M * t;
+    c.M *= q;
+}
+
+// c (a class of doubling_class, M != 0) narrowed by the q-th power
+// character of q = rare_q_of(p, ...) (0: unchanged): with z = 2^-(p-1)/q
+// and y = wt^((p-1)/q), either z = 1 (no condition, or no zero at all when
+// y != 1) or n = log_z y (mod q).
+CTD_HD PowerClass refine_class(const Mont &m, uint64_t k, bool negate, PowerClass c, uint32_t q)
+{
+    if (!c.M || !q)
+        return c;
+    uint64_t z, y;
+    power_pair(m, k, negate, (m.p - 1) / q, z, y);
+    if (z == m.one)
+        return y == m.one ? c : PowerClass{0, 0};
+    const uint32_t j = small_log(m, z, y, q);
+    if (j < q)  // always, for prime p
+        crt_merge_small(c, j, q);
     return c;
 }
 

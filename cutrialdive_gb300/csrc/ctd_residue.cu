@@ -1578,10 +1578,17 @@ residue_kernel(JobView job, const uint64_t *__restrict__ primes, uint64_t nprime
 //                    (prime, tile) items from a counter, so a warp's lanes
 //                    walk classes of the same M -- equal lengths, no lane
 //                    waiting on a longer one.
-// The classes are the divisors of 2^6 * 105 (56 of them), ranked by size.
-// rank of M among the divisors of 2^3 * 3 * 5 * 7
+// Buckets rank the classes by M: M <= 840 by the number of divisors of 840
+// below it (a divisor's own rank; a class with a rare prime, M = 11, 22, 13,
+// ..., shares the bucket of the next divisor), M above 840 by half octaves.
 __device__ __forceinline__ uint32_t class_bucket(uint32_t M)
 {
+    if (M > 840) {
+        const uint32_t b = 31 - __clz(M);  // 9 .. 15
+        const uint32_t h = (uint64_t)M * M >= (2ull << (2 * b)) ? 1u : 0u;
+        const uint32_t f = 2 * b + h;  // 19 .. 31
+        return 32 + (f - 19 < CLASS_BUCKETS - 33 ? f - 19 : CLASS_BUCKETS - 33);
+    }
     uint32_t rank = 0;
 #pragma unroll
     for (int i = 0; i <= POWRES_MAX_2EXP; ++i)
@@ -1593,14 +1600,56 @@ __device__ __forceinline__ uint32_t class_bucket(uint32_t M)
     return rank;
 }
 
+// the largest rare prime of a job's refinement
+__device__ __forceinline__ uint32_t refine_qmax(const JobView &job) { return job.refine_q ? job.refine_q : 61u; }
+
+// whether a classified prime goes to the rare-prime refinement
+__device__ __forceinline__ bool wants_refine(const JobView &job, uint64_t p, uint32_t code)
+{
+    return code && p < (1ull << 63) && rare_q_of(p, refine_qmax(job)) != 0;
+}
+
+// the refined code of a classified prime (0: it divides no term)
+template <uint32_t FAM>
+__device__ __forceinline__ uint32_t refined_code(const JobView &job, uint64_t p, uint32_t code)
+{
+    const uint64_t k = FAM == MERSENNE ? 1 : (job.param < p ? job.param : job.param % p);
+    Mont m;
+    m.init(p);
+    const PowerClass c = refine_class(m, k, FAM == PROTH, PowerClass{code >> 16, code & 0xffffu},
+                                      rare_q_of(p, refine_qmax(job)));
+    return c.M ? (c.M << 16) | c.r : 0u;
+}
+
 template <uint32_t FAM>
 __global__ void __launch_bounds__(256) classify_kernel(JobView job, const uint64_t *__restrict__ primes,
                                                        uint64_t nprimes, uint32_t *__restrict__ codes,
-                                                       ClassCounters *__restrict__ cc)
+                                                       ClassCounters *__restrict__ cc, uint32_t *__restrict__ refine)
 {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nprimes; i += stride) {
-        const uint32_t code = doubling_class_code<FAM>(job, primes[i]);
+        const uint64_t p = primes[i];
+        const uint32_t code = doubling_class_code<FAM>(job, p);
+        codes[i] = code;
+        if (wants_refine(job, p, code))
+            refine[aggregated_increment(&cc->nrefine, 0)] = (uint32_t)i;
+        else if (code)
+            aggregated_increment(cc->count, class_bucket(code >> 16));
+    }
+}
+
+// The rare-prime refinement over the primes classify listed (compacted, so
+// every lane of a warp does the same two powers)
+template <uint32_t FAM>
+__global__ void __launch_bounds__(256) refine_kernel(JobView job, const uint64_t *__restrict__ primes,
+                                                     uint32_t *__restrict__ codes, ClassCounters *__restrict__ cc,
+                                                     const uint32_t *__restrict__ refine)
+{
+    const uint32_t n = cc->nrefine;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+        const uint32_t i = refine[t];
+        const uint32_t code = refined_code<FAM>(job, primes[i], codes[i]);
         codes[i] = code;
         if (code)
             aggregated_increment(cc->count, class_bucket(code >> 16));
@@ -2128,6 +2177,7 @@ void residue_scratch_destroy(ResidueScratch *rs)
         return;
     cudaFree(rs->codes);
     cudaFree(rs->items);
+    cudaFree(rs->refine);
     cudaFree(rs->counters);
     delete rs;
 }
@@ -2145,12 +2195,16 @@ static int ensure_class_scratch(ResidueScratch *rs, uint64_t nprimes, std::strin
         return CTD_OK;
     cudaFree(rs->codes);
     cudaFree(rs->items);
+    cudaFree(rs->refine);
     rs->codes = nullptr;
     rs->items = nullptr;
+    rs->refine = nullptr;
     rs->cap = 0;
     cudaError_t e = cudaMalloc(&rs->codes, nprimes * sizeof(uint32_t));
     if (e == cudaSuccess)
         e = cudaMalloc(&rs->items, nprimes * sizeof(ClassItem));
+    if (e == cudaSuccess)
+        e = cudaMalloc(&rs->refine, nprimes * sizeof(uint32_t));
     if (e != cudaSuccess) {
         err = std::string("class scratch: ") + cudaGetErrorString(e);
         return e == cudaErrorMemoryAllocation ? CTD_ERR_OUT_OF_MEMORY : CTD_ERR_CUDA;
@@ -2181,7 +2235,15 @@ static int launch_classified(const JobView &v, const uint64_t *d_primes, uint64_
     const uint64_t want = (n + 255) / 256;
     const int cgrid = (int)(want < (uint64_t)rs->sm_count * 8 ? want : (uint64_t)rs->sm_count * 8);
     if (e == cudaSuccess) {
-        classify_kernel<FAM><<<cgrid, 256, 0, st>>>(v, d_primes, n, rs->codes, rs->counters);
+        classify_kernel<FAM><<<cgrid, 256, 0, st>>>(v, d_primes, n, rs->codes, rs->counters, rs->refine);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        note_kernel_launch();
+        // the listed primes are about a quarter of n: a grid for that many
+        const uint64_t rwant = (n / 4 + 255) / 256;
+        const int rgrid = (int)(rwant < (uint64_t)rs->sm_count * 8 ? (rwant ? rwant : 1) : (uint64_t)rs->sm_count * 8);
+        refine_kernel<FAM><<<rgrid, 256, 0, st>>>(v, d_primes, rs->codes, rs->counters, rs->refine);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) {

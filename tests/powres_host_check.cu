@@ -1,7 +1,9 @@
 // Host-side check of the doubling families' power-residue classes
 // (ctd_powres.cuh is __host__ __device__).  Reads "p wt" lines on stdin
-// (odd prime p, 0 < wt < p) and prints "M r": every n with 2^-n = wt (mod p)
-// satisfies n = r (mod M); M = 0 when no n does.
+// (odd prime p, 0 < wt < p) and prints "M r M2 r2": every n with
+// 2^-n = wt (mod p) satisfies n = r (mod M), and n = r2 (mod M2) after the
+// refinement by the smallest rare prime q = 11 .. 61 dividing p - 1; M = 0 (M2 = 0)
+// when no n does.
 #include <cinttypes>
 #include <cstdio>
 
@@ -15,7 +17,8 @@ int main()
         m.init(p);
         // wt as -k with k = p - wt (the Proth form); the test covers every wt
         const ctd::PowerClass c = ctd::doubling_class(m, p - wt, true);
-        std::printf("%u %u\n", c.M, c.r);
+        const ctd::PowerClass f = ctd::refine_class(m, p - wt, true, c, ctd::rare_q_of(p, 61));
+        std::printf("%u %u %u %u\n", c.M, c.r, f.M, f.r);
     }
     return 0;
 }

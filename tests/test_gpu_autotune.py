@@ -49,21 +49,25 @@ def test_autotune_keeps_results(eng, case):
 
 @pytest.mark.parametrize("family,param", [(O.PROTH, 3), (O.MERSENNE, 0), (O.RIESEL, 999_999)])
 def test_classes_on_and_off_same_factors(eng, family, param):
-    """classify_min (the autotuner's power-residue switch) changes only the speed."""
+    """classify_min (the autotuner's power-residue switch) and refine_q (the
+    rare primes of the classes' refinement: none, up to 31, all) change only
+    the speed."""
     n0, n1, f0, f1 = 1, 9001, (1 << 33) - (1 << 21), (1 << 33) + (1 << 21)
     job = ctd.CtdJob(family, 32, param, n0, n1, f0, f1)
     outs = []
     try:
-        for cm in (1, 0xFFFFFFFF):
+        for cm, rq in ((1, 0), (1, 1), (1, 31), (0xFFFFFFFF, 0)):
             t = eng.get_tuning(family)
             t["classify_min"] = cm
+            t["refine_q"] = rq
             eng.set_tuning_for(family, f0.bit_length(), t)
             eng.set_tuning_for(family, f1.bit_length(), t)
             outs.append(run(eng, job))
     finally:
         eng.set_tuning_for(family, f0.bit_length(), None)
         eng.set_tuning_for(family, f1.bit_length(), None)
-    assert outs[0] == outs[1] == O.trial_factor(family, param, n0, n1, f0, f1, 32).format()
+    want = O.trial_factor(family, param, n0, n1, f0, f1, 32).format()
+    assert all(o == want for o in outs)
 
 
 def test_set_tuning_rejects_bad_values(eng):

@@ -1,8 +1,10 @@
 """The doubling families' power-residue classes (ctd_powres.cuh), run on the
 host from the kernel's own source and checked with Python integers: every
 n with 2^-n = wt (mod p) -- a zero of k*2^n-+1 or 2^n-1 -- lies in the class
-n = r (mod M) the kernel walks, and a prime classed as dividing no term
-(M = 0) really divides none (wt is outside the subgroup generated by 2)."""
+n = r (mod M) the kernel walks, both the class of the 2^3-, 3rd-, 5th- and
+7th-power characters and its refinement by the smallest rare prime 11..61
+dividing p - 1, and a prime classed as dividing no term (M = 0) really divides none
+(wt is outside the subgroup generated by 2)."""
 import os
 import random
 import shutil
@@ -31,12 +33,18 @@ def classes(checker, cases):
     return [tuple(map(int, line.split())) for line in out[:len(cases)]]
 
 
+def both(got):
+    """(M, r) of the base class and of the refined one, for each case"""
+    return [((M, r), (M2, r2)) for M, r, M2, r2 in got]
+
+
 def primes_for_test():
     rnd = random.Random(11)
     ps = [3, 5, 7, 11, 13, 17, 31, 41, 43, 97, 113, 193, 211, 257, 421, 631, 641, 1009, 2017, 65537, 3 * 2**30 + 1,
           15 * 2**27 + 1, 7 * 2**26 + 1, 2**31 - 1, 1000000007, 2**32 + 15]
     # primes with p - 1 divisible by large powers of 2 and by 3 * 5 * 7
-    for m in (2**10 * 105, 2**8 * 105, 105, 64 * 3, 64 * 35):
+    for m in (2**10 * 105, 2**8 * 105, 105, 64 * 3, 64 * 35, 11 * 13 * 105, 8 * 17 * 19, 23 * 29 * 31, 37 * 41,
+              43 * 47 * 8, 53 * 59 * 61, 61 * 11):
         k = rnd.randrange(1, 2**22)
         while len([q for q in ps if q % m == 1]) < 8:
             if sympy.isprime(k * m + 1):
@@ -56,37 +64,47 @@ def test_every_zero_lies_in_the_class(checker):
         for w in {1, p - 1, p - 3 % p if p > 3 else 1, rnd.randrange(1, p), rnd.randrange(1, p)}:
             if 0 < w < p:
                 cases.append((p, w))
-    got = classes(checker, cases)
-    skipped = 0
-    for (p, w), (M, r) in zip(cases, got):
+    got = both(classes(checker, cases))
+    skipped = refined = 0
+    for (p, w), cls in zip(cases, got):
         h = pow(2, -1, p)
         order = int(sympy.n_order(2, p))
         member = pow(w, order, p) == 1  # w in <2^-1> = <2>
-        if M == 0:
-            assert not member, (p, w)
-            skipped += 1
-            continue
-        assert 0 <= r < M and order % M == 0, (p, w, M, r)
-        if member:
-            n = int(sympy.discrete_log(p, w, h))
-            assert pow(h, n, p) == w
-            assert n % M == r, (p, w, M, r, n)
-    assert skipped > 0
+        (M0, r0), (M2, r2) = cls
+        if M0 and M2:
+            assert M2 % M0 == 0 and r2 % M0 == r0, (p, w, cls)  # a sub-class
+            refined += M2 > M0
+        elif M0:
+            refined += 1
+        else:
+            assert M2 == 0, (p, w, cls)
+        for M, r in cls:
+            if M == 0:
+                assert not member, (p, w)
+                skipped += 1
+                continue
+            assert 0 <= r < M <= 65535 and order % M == 0, (p, w, M, r)
+            if member:
+                n = int(sympy.discrete_log(p, w, h))
+                assert pow(h, n, p) == w
+                assert n % M == r, (p, w, M, r, n)
+    assert skipped > 0 and refined > 20, (skipped, refined)
 
 
 def test_small_primes_exhaustively(checker):
     """Every prime below 600 and every target: the class holds all zeros of
     one full period, and M = 0 exactly when there are none."""
     cases = [(p, w) for p in map(int, sympy.primerange(3, 600)) for w in range(1, p)]
-    got = classes(checker, cases)
-    for (p, w), (M, r) in zip(cases, got):
+    got = both(classes(checker, cases))
+    for (p, w), cls in zip(cases, got):
         h = pow(2, -1, p)
         order = int(sympy.n_order(2, p))
         zeros = [n for n in range(order) if pow(h, n, p) == w]
-        if M == 0:
-            assert zeros == [], (p, w)
-        else:
-            assert all(n % M == r for n in zeros), (p, w, M, r, zeros)
+        for M, r in cls:
+            if M == 0:
+                assert zeros == [], (p, w)
+            else:
+                assert all(n % M == r for n in zeros), (p, w, M, r, zeros)
 
 
 def test_class_keeps_a_small_fraction_of_terms(checker):
@@ -98,6 +116,10 @@ def test_class_keeps_a_small_fraction_of_terms(checker):
     while len(ps) < 3000:
         x = int(sympy.nextprime(x))
         ps.append(x)
-    got = classes(checker, [(p, p - 3) for p in ps])
-    frac = sum(1 / M for M, _ in got if M) / len(ps)
+    got = both(classes(checker, [(p, p - 3) for p in ps]))
+    frac = sum(1 / M for (M, _), _ in got if M) / len(ps)
     assert 0.10 < frac < 0.22, frac
+    # the rare primes 11..61 take it down by about prod(1 - 1/q) = 0.58 (the
+    # smallest one of each prime: 0.58 as well)
+    frac2 = sum(1 / M for _, (M, _) in got if M) / len(ps)
+    assert 0.50 < frac2 / frac < 0.68, (frac, frac2)
