@@ -114,7 +114,7 @@ struct ClassCounters {
     uint32_t fill[CLASS_BUCKETS];   // regroup cursors
     unsigned long long next;        // walk work counter
     uint32_t nrefine;               // primes listed for the rare-prime refinement
-    uint32_t pad;
+    uint32_t nlisted;               // primes the quadratic screen left for classification
 };
 // a prime with its class code (M << 16 | r)
 struct ClassItem {
@@ -128,6 +128,7 @@ struct ResidueScratch {
     uint32_t *codes = nullptr;
     ClassItem *items = nullptr;
     uint32_t *refine = nullptr;  // indices of the primes to refine
+    uint32_t *listed = nullptr;  // indices of the primes to classify
     uint64_t cap = 0;  // primes
     ClassCounters *counters = nullptr;
 };

@@ -41,15 +41,23 @@ struct PowerClass {
     uint32_t r;  // < M
 };
 
-// n = r (mod M) and n = j (mod q), gcd(M, q) = 1  ->  one class mod M q
-CTD_HD void crt_merge(PowerClass &c, uint32_t j, uint32_t q)
+// n = r (mod M) and n = j (mod q) for a prime q <= 64 not dividing M:
+// n = r + M t with t = (j - r) M^-1 (mod q), the inverse by Fermat
+// (M^(q-2)); 32-bit arithmetic
+CTD_HD void crt_merge_small(PowerClass &c, uint32_t j, uint32_t q)
 {
-    uint32_t t = 0;
-    while ((c.r + (uint64_t)c.M * t) % q != j)
-        ++t;
+    const uint32_t d = c.M % q;
+    uint32_t inv = 1, b = d;
+    for (uint32_t e = q - 2; e; e >>= 1) {
+        if (e & 1)
+            inv = inv * b % q;
+        b = b * b % q;
+    }
+    const uint32_t t = (j + q - c.r % q) % q * inv % q;
     c.r += c.M * t;
     c.M *= q;
 }
+
 
 // The classifier's fixed chains multiply through one out-of-line function
 // on the device (the two powering loops keep theirs inline): with all ~140
@@ -115,6 +123,78 @@ CTD_HD Pow105 pow105(const Mont &m, uint64_t x)
     const uint64_t x10 = mul(x5, x5), x15 = mul(x10, x5), x14 = mul(x7, x7), x21 = mul(x14, x7);
     const uint64_t x35 = mul(x21, x14), x70 = mul(x35, x35), x105 = mul(x70, x35);
     return Pow105{x15, x21, x35, x105};
+}
+
+// ---- the quadratic screen
+// The classes' cheapest condition needs no power: when 2 is a quadratic
+// residue mod p (p = +-1 mod 8) every 2^-n is one, so a target wt that is a
+// non-residue is never reached -- p divides no term.  That is a quarter of
+// the primes for a generic target, decided by Legendre symbols alone, so the
+// kernels take those primes out before the two powers of doubling_class.
+
+CTD_HD int ctz64(uint64_t x)
+{
+#ifdef __CUDA_ARCH__
+    return __ffsll((long long)x) - 1;
+#else
+    return __builtin_ctzll(x);
+#endif
+}
+
+// Jacobi symbol (a/n) for odd n: a reduced mod n once, then the binary
+// algorithm (factors of 2 by (2/n) = -1 iff n = 3, 5 mod 8; quadratic
+// reciprocity on each swap; subtraction)
+CTD_HD int jacobi(uint64_t a, uint64_t n)
+{
+    a %= n;
+    int t = 1;
+    while (a) {
+        const int z = ctz64(a);
+        a >>= z;
+        if ((z & 1) && ((n & 7) == 3 || (n & 7) == 5))
+            t = -t;
+        if (a < n) {
+            if ((a & 3) == 3 && (n & 3) == 3)
+                t = -t;
+            const uint64_t x = a;
+            a = n;
+            n = x;
+        }
+        a -= n;
+    }
+    return n == 1 ? t : 0;
+}
+
+// The Legendre symbol (wt/p), wt = -k (negate) or k, for an odd prime p
+// and k < 2^64: (2/p)^s (k'/p) (-1/p)^negate with k = 2^s k', and
+// (k'/p) = (p/k') (-1)^((k'-1)/2 (p-1)/2) by reciprocity -- a reduction of p
+// mod k' and a Jacobi symbol of k'-sized numbers.  0 when p | k.
+CTD_HD int target_symbol(uint64_t p, uint64_t k, bool negate)
+{
+    const uint64_t kr = k < p ? k : k % p;
+    if (!kr)
+        return 0;
+    const int s = ctz64(kr);
+    const uint64_t k1 = kr >> s;
+    const bool two_nr = (p & 7) == 3 || (p & 7) == 5;  // (2/p) = -1
+    int t = (s & 1) && two_nr ? -1 : 1;
+    if (k1 > 1) {
+        t *= jacobi(p, k1);
+        if ((k1 & 3) == 3 && (p & 3) == 3)
+            t = -t;
+    }
+    if (negate && (p & 3) == 3)  // (-1/p) = -1
+        t = -t;
+    return t;
+}
+
+// true when the quadratic characters alone show that 2^-n = wt (mod p) has
+// no solution (2 a residue, wt a non-residue), or p | k
+CTD_HD bool quadratic_excluded(uint64_t p, uint64_t k, bool negate)
+{
+    const bool two_qr = (p & 7) == 1 || (p & 7) == 7;
+    const int t = target_symbol(p, k, negate);
+    return t == 0 || (two_qr && t < 0);
 }
 
 // A = 2^-e = 2^(p - 1 - e) (left-to-right, a set bit a doubling) and B =
@@ -202,21 +282,23 @@ CTD_HD PowerClass doubling_class(const Mont &m, uint64_t k, bool negate)
         for (uint32_t jj = 0; jj < (1u << POWRES_MAX_2EXP); ++jj) {
             if (jj < (1u << i) && t == y)
                 j = jj;
-            t = mul(t, z);
+            if (jj + 1 < (1u << POWRES_MAX_2EXP))
+                t = mul(t, z);
         }
         c.M = 1u << i;
         c.r = j;
     }
-    // ---- q = 3, 5, 7: z = A^(2^u 105 / q)
-    uint64_t A2 = A, B2 = B;  // A^(2^u), B^(2^u): loops of fixed length
+    // ---- q = 3, 5, 7: z = A^(2^u 105 / q) = (A^(105/q))^(2^u), squarings
+    // of the chain's values (a loop of fixed length)
+    uint64_t zq[3] = {pa.p35, pa.p21, pa.p15}, yq[3] = {pb.p35, pb.p21, pb.p15};
 #pragma unroll
-    for (int t = 0; t < POWRES_MAX_2EXP; ++t) {
-        const uint64_t a2 = mul(A2, A2), b2 = mul(B2, B2);
-        A2 = t < u ? a2 : A2;
-        B2 = t < u ? b2 : B2;
-    }
-    const Pow105 qa = pow105(m, A2), qb = pow105(m, B2);
-    const uint64_t zq[3] = {qa.p35, qa.p21, qa.p15}, yq[3] = {qb.p35, qb.p21, qb.p15};
+    for (int t = 0; t < POWRES_MAX_2EXP; ++t)
+#pragma unroll
+        for (int kq = 0; kq < 3; ++kq) {
+            const uint64_t z2 = mul(zq[kq], zq[kq]), y2 = mul(yq[kq], yq[kq]);
+            zq[kq] = t < u ? z2 : zq[kq];
+            yq[kq] = t < u ? y2 : yq[kq];
+        }
     const uint32_t qs[3] = {3, 5, 7};
 #pragma unroll
     for (int kq = 0; kq < 3; ++kq) {
@@ -229,14 +311,16 @@ CTD_HD PowerClass doubling_class(const Mont &m, uint64_t k, bool negate)
         }
         uint32_t j = q;
         uint64_t t = m.one;
+#pragma unroll
         for (uint32_t jj = 0; jj < q; ++jj) {
             if (t == y)
                 j = jj;
-            t = mul(t, z);
+            if (jj + 1 < q)
+                t = mul(t, z);
         }
         if (j >= q)  // cannot happen for prime p (y is a q-th root of unity)
             return PowerClass{1, 0};
-        crt_merge(c, j, q);
+        crt_merge_small(c, j, q);
     }
     return c;
 }
@@ -304,23 +388,6 @@ CTD_HD uint32_t small_log(const Mont &m, uint64_t z, uint64_t y, uint32_t q)
         t = mul(t, g);
     }
     return found;
-}
-
-// n = r (mod M) and n = j (mod q) for a prime q <= 64 not dividing M:
-// n = r + M t with t = (j - r) M^-1 (mod q), the inverse by Fermat
-// (M^(q-2)); 32-bit arithmetic
-CTD_HD void crt_merge_small(PowerClass &c, uint32_t j, uint32_t q)
-{
-    const uint32_t d = c.M % q;
-    uint32_t inv = 1, b = d;
-    for (uint32_t e = q - 2; e; e >>= 1) {
-        if (e & 1)
-            inv = inv * b % q;
-        b = b * b % q;
-    }
-    const uint32_t t = (j + q - c.r % q) % q * inv % q;
-    c.r += c.M * t;
-    c.M *= q;
 }
 
 // c (a class of doubling_class, M != 0) narrowed by the q-th power

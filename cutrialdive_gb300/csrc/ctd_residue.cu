@@ -1621,13 +1621,35 @@ __device__ __forceinline__ uint32_t refined_code(const JobView &job, uint64_t p,
     return c.M ? (c.M << 16) | c.r : 0u;
 }
 
+// The quadratic screen (Proth, Riesel): the primes whose target is a
+// quadratic non-residue while 2 is a residue (a quarter of them) divide no
+// term and get code 0 here; the others are listed for classify_kernel, so
+// its warps spend the two powers on primes that need them.
 template <uint32_t FAM>
-__global__ void __launch_bounds__(256) classify_kernel(JobView job, const uint64_t *__restrict__ primes,
-                                                       uint64_t nprimes, uint32_t *__restrict__ codes,
-                                                       ClassCounters *__restrict__ cc, uint32_t *__restrict__ refine)
+__global__ void __launch_bounds__(256) screen_kernel(JobView job, const uint64_t *__restrict__ primes,
+                                                     uint64_t nprimes, uint32_t *__restrict__ codes,
+                                                     ClassCounters *__restrict__ cc, uint32_t *__restrict__ listed)
 {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nprimes; i += stride) {
+        if (quadratic_excluded(primes[i], job.param, FAM == PROTH))
+            codes[i] = 0;
+        else
+            listed[aggregated_increment(&cc->nlisted, 0)] = (uint32_t)i;
+    }
+}
+
+// the classes of the listed primes (all primes when `listed` is null)
+template <uint32_t FAM>
+__global__ void __launch_bounds__(256, 4) classify_kernel(JobView job, const uint64_t *__restrict__ primes,
+                                                       uint64_t nprimes, uint32_t *__restrict__ codes,
+                                                       ClassCounters *__restrict__ cc, uint32_t *__restrict__ refine,
+                                                       const uint32_t *__restrict__ listed)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t n = listed ? cc->nlisted : nprimes;
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+        const uint64_t i = listed ? listed[t] : t;
         const uint64_t p = primes[i];
         const uint32_t code = doubling_class_code<FAM>(job, p);
         codes[i] = code;
@@ -2178,6 +2200,7 @@ void residue_scratch_destroy(ResidueScratch *rs)
     cudaFree(rs->codes);
     cudaFree(rs->items);
     cudaFree(rs->refine);
+    cudaFree(rs->listed);
     cudaFree(rs->counters);
     delete rs;
 }
@@ -2196,15 +2219,19 @@ static int ensure_class_scratch(ResidueScratch *rs, uint64_t nprimes, std::strin
     cudaFree(rs->codes);
     cudaFree(rs->items);
     cudaFree(rs->refine);
+    cudaFree(rs->listed);
     rs->codes = nullptr;
     rs->items = nullptr;
     rs->refine = nullptr;
+    rs->listed = nullptr;
     rs->cap = 0;
     cudaError_t e = cudaMalloc(&rs->codes, nprimes * sizeof(uint32_t));
     if (e == cudaSuccess)
         e = cudaMalloc(&rs->items, nprimes * sizeof(ClassItem));
     if (e == cudaSuccess)
         e = cudaMalloc(&rs->refine, nprimes * sizeof(uint32_t));
+    if (e == cudaSuccess)
+        e = cudaMalloc(&rs->listed, nprimes * sizeof(uint32_t));
     if (e != cudaSuccess) {
         err = std::string("class scratch: ") + cudaGetErrorString(e);
         return e == cudaErrorMemoryAllocation ? CTD_ERR_OUT_OF_MEMORY : CTD_ERR_CUDA;
@@ -2234,8 +2261,16 @@ static int launch_classified(const JobView &v, const uint64_t *d_primes, uint64_
     cudaError_t e = cudaMemsetAsync(rs->counters, 0, sizeof(ClassCounters), st);
     const uint64_t want = (n + 255) / 256;
     const int cgrid = (int)(want < (uint64_t)rs->sm_count * 8 ? want : (uint64_t)rs->sm_count * 8);
+    // the quadratic screen (Mersenne's target 1 is always a residue)
+    uint32_t *listed = FAM == MERSENNE ? nullptr : rs->listed;
+    if (e == cudaSuccess && listed) {
+        screen_kernel<FAM><<<cgrid, 256, 0, st>>>(v, d_primes, n, rs->codes, rs->counters, listed);
+        e = cudaGetLastError();
+        if (e == cudaSuccess)
+            note_kernel_launch();
+    }
     if (e == cudaSuccess) {
-        classify_kernel<FAM><<<cgrid, 256, 0, st>>>(v, d_primes, n, rs->codes, rs->counters, rs->refine);
+        classify_kernel<FAM><<<cgrid, 256, 0, st>>>(v, d_primes, n, rs->codes, rs->counters, rs->refine, listed);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) {
@@ -2276,7 +2311,9 @@ int launch_residues(const JobView &view, const uint64_t *d_primes, uint64_t npri
         return CTD_OK;
     const bool doubling = view.family == PROTH || view.family == RIESEL || view.family == MERSENNE;
     const uint32_t cmin = view.classify_min ? view.classify_min : DEFAULT_CLASSIFY_MIN;
-    if (scratch && doubling && view.variant == CTD_VARIANT_AUTO && view.n1 - view.n0 >= cmin) {
+    // (the class passes index the primes with 32 bits)
+    if (scratch && doubling && view.variant == CTD_VARIANT_AUTO && view.n1 - view.n0 >= cmin &&
+        nprimes <= 0xffffffffull) {
         switch (view.family) {
         case PROTH: return launch_classified<PROTH>(view, d_primes, nprimes, stream, scratch, err);
         case RIESEL: return launch_classified<RIESEL>(view, d_primes, nprimes, stream, scratch, err);

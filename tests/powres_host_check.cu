@@ -3,7 +3,8 @@
 // (odd prime p, 0 < wt < p) and prints "M r M2 r2": every n with
 // 2^-n = wt (mod p) satisfies n = r (mod M), and n = r2 (mod M2) after the
 // refinement by the smallest rare prime q = 11 .. 61 dividing p - 1; M = 0 (M2 = 0)
-// when no n does.
+// when no n does; then "x" (1 when the quadratic screen excludes p) and the
+// Jacobi symbol (wt/p).
 #include <cinttypes>
 #include <cstdio>
 
@@ -18,7 +19,8 @@ int main()
         // wt as -k with k = p - wt (the Proth form); the test covers every wt
         const ctd::PowerClass c = ctd::doubling_class(m, p - wt, true);
         const ctd::PowerClass f = ctd::refine_class(m, p - wt, true, c, ctd::rare_q_of(p, 61));
-        std::printf("%u %u %u %u\n", c.M, c.r, f.M, f.r);
+        const int x = ctd::quadratic_excluded(p, p - wt, true) ? 1 : 0;
+        std::printf("%u %u %u %u %d %d\n", c.M, c.r, f.M, f.r, x, ctd::jacobi(wt, p));
     }
     return 0;
 }

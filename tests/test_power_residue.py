@@ -35,7 +35,30 @@ def classes(checker, cases):
 
 def both(got):
     """(M, r) of the base class and of the refined one, for each case"""
-    return [((M, r), (M2, r2)) for M, r, M2, r2 in got]
+    return [((M, r), (M2, r2)) for M, r, M2, r2, _, _ in got]
+
+
+def test_quadratic_screen_and_jacobi(checker):
+    """The Jacobi symbol of the screen equals sympy's, and every prime the
+    quadratic screen excludes is one the classes find dividing no term."""
+    rnd = random.Random(7)
+    cases = []
+    for p in primes_for_test():
+        for w in {1, 2, p - 1, p - 2, p - 3 % p if p > 3 else 1, rnd.randrange(1, p), rnd.randrange(1, p)}:
+            if 0 < w < p:
+                cases.append((p, w))
+    cases += [(p, w) for p in map(int, sympy.primerange(3, 200)) for w in range(1, p)]
+    got = classes(checker, cases)
+    screened = 0
+    for (p, w), (M, _, M2, _, x, jac) in zip(cases, got):
+        assert jac == sympy.jacobi_symbol(w, p), (p, w, jac)
+        if x:
+            screened += 1
+            assert M == 0 and M2 == 0, (p, w)
+            assert p % 8 in (1, 7) and jac == -1, (p, w)
+        else:
+            assert not (p % 8 in (1, 7) and jac == -1), (p, w)
+    assert screened > len(cases) // 8
 
 
 def primes_for_test():
@@ -116,7 +139,11 @@ def test_class_keeps_a_small_fraction_of_terms(checker):
     while len(ps) < 3000:
         x = int(sympy.nextprime(x))
         ps.append(x)
-    got = both(classes(checker, [(p, p - 3) for p in ps]))
+    raw = classes(checker, [(p, p - 3) for p in ps])
+    # the quadratic screen takes out about a quarter of the primes (of the
+    # 43 % that divide no term)
+    assert 0.20 < sum(g[4] for g in raw) / len(ps) < 0.30
+    got = both(raw)
     frac = sum(1 / M for (M, _), _ in got if M) / len(ps)
     assert 0.10 < frac < 0.22, frac
     # the rare primes 11..61 take it down by about prod(1 - 1/q) = 0.58 (the
