@@ -654,36 +654,55 @@ __device__ __forceinline__ uint64_t doubling_target_of(const JobView &job, uint6
 // The doubling walk over n = r (mod M) in [s, e), p < 2^63.  One body for
 // the three families (they differ only in the target), so the kernels that
 // walk classes of several families hold one copy of it.
+// 2^-x in Montgomery form: left-to-right powering of 2^-1, each set bit a
+// halving of the Montgomery representative ((x R) / 2 = (x / 2) R) -- as many
+// squarings as x has bits
+__device__ __forceinline__ uint64_t pow_half(const Mont &m, uint64_t x)
+{
+    uint64_t h = m.one;
+    for (int b = 63 - clz64(x | 1); b >= 0; --b) {
+        h = m.mul(h, h);
+        if ((x >> b) & 1)
+            h = half63(h, m.p);
+    }
+    return h;
+}
+
+// x mod M, x / M for a class modulus M < 2^16 (32-bit division when x fits)
+__device__ __forceinline__ uint32_t mod_small(uint64_t x, uint32_t M)
+{
+    return x >> 32 ? (uint32_t)(x % M) : (uint32_t)x % M;
+}
+__device__ __forceinline__ uint64_t div_small(uint64_t x, uint32_t M)
+{
+    return x >> 32 ? x / M : (uint32_t)x / M;
+}
+
 __device__ void run_doubling_class(const JobView &job, uint64_t p, uint32_t M, uint32_t r, uint64_t s, uint64_t e)
 {
-    const uint32_t sr = (uint32_t)(s % M);
+    const uint32_t sr = mod_small(s, M);
     const uint64_t off = r >= sr ? r - sr : M - sr + r;
     if (off >= e - s)
         return;
-    const uint64_t nf = s + off;               // first term of the class
-    const uint64_t cnt = (e - 1 - nf) / M + 1;  // terms nf, nf + M, ... below e
+    const uint64_t nf = s + off;                   // first term of the class
+    const uint64_t cnt = div_small(e - 1 - nf, M) + 1;  // terms nf, nf + M, ... below e
+    // Shoup quotients straight from Montgomery forms: for W = w R mod p,
+    // floor(w 2^64 / p) = (w 2^64 - W) / p = W (-p^-1) mod 2^64 = W pinv
+    // (exact: the quotient is below 2^64), so no R^2 is needed
     Mont m;
-    m.init(p);
+    m.init_lite(p);
     const uint64_t wt = doubling_target_of(job, p);
     const uint64_t nr = nf < p - 1 ? nf : nf % (p - 1);
-    uint64_t w = m.from(m.pow2(p - 1 - nr));  // 2^-nf (Fermat)
-    // 2^-M in Montgomery form: left-to-right powering of 2^-1, each set bit a
-    // halving of the Montgomery representative ((x R) / 2 = (x / 2) R)
-    uint64_t HM = m.one;
-    for (int b = 31 - __clz(M); b >= 0; --b) {
-        HM = m.mul(HM, HM);
-        if ((M >> b) & 1)
-            HM = half63(HM, p);
-    }
-    const uint64_t g = m.from(HM);
-    const MulConst step{g, m.shoup(g)};  // w -> w 2^-M: the next term of the class
+    uint64_t w = m.from(pow_half(m, nr));  // 2^-nf
+    const uint64_t HM = pow_half(m, M);    // 2^-M in Montgomery form
+    const MulConst step{m.from(HM), HM * m.pinv};  // w -> w 2^-M: the next term of the class
     const uint64_t at0 = nf - job.n0;
     uint64_t i = 0;
     if (cnt >= 2 * BS) {
         // targets wt 2^(M j), j < 32: term j of a block is a zero iff the
         // block's state equals target j
-        const uint64_t c = m.from(m.pow2(M));
-        const MulConst up{c, m.shoup(c)};
+        const uint64_t C = m.pow2(M);
+        const MulConst up{m.from(C), C * m.pinv};
         uint32_t tlo[BS];
         uint64_t t = wt;
 #pragma unroll
@@ -713,8 +732,8 @@ __device__ void run_doubling_class(const JobView &job, uint64_t p, uint32_t M, u
                                [&](uint64_t x) { return redc32(redc32(x, plo, phi, pinv32, one), plo, phi, pinv32, one); },
                                replay);
         } else {
-            const uint64_t G = m.from(square_n(m, HM, 5));  // 2^-32M
-            const MulConst giant{G, m.shoup(G)};
+            const uint64_t G = square_n(m, HM, 5);  // 2^-32M in Montgomery form
+            const MulConst giant{m.from(G), G * m.pinv};
             w = run_blocks(tlo, w, nb, [&](uint64_t x) { return giant.mul(x, p); }, replay);
         }
         i = nb * BS;
@@ -1678,27 +1697,50 @@ __global__ void __launch_bounds__(256) refine_kernel(JobView job, const uint64_t
     }
 }
 
+// Each CTA regroups tiles of 256 x REGROUP_PER_THREAD primes: a histogram of
+// the tile's classes in shared memory, one global atomic per class and tile
+// to reserve the tile's places in the class, then the scatter.  (One global
+// atomic per class and warp, as first written, left the kernel waiting on
+// atomics: long-scoreboard stalls of ~140 cycles per instruction.)
+constexpr int REGROUP_PER_THREAD = 16;
 __global__ void __launch_bounds__(256) regroup_kernel(const uint64_t *__restrict__ primes, uint64_t nprimes,
                                                       const uint32_t *__restrict__ codes, ClassCounters *__restrict__ cc,
                                                       ClassItem *__restrict__ items)
 {
-    __shared__ uint32_t base[CLASS_BUCKETS];
-    if (threadIdx.x == 0) {
+    __shared__ uint32_t base[CLASS_BUCKETS];       // first place of each class
+    __shared__ uint32_t hist[CLASS_BUCKETS];       // the tile's primes per class
+    __shared__ uint32_t tile_base[CLASS_BUCKETS];  // the tile's first place per class
+    const uint32_t tid = threadIdx.x;
+    if (tid < CLASS_BUCKETS) {
         uint32_t run = 0;
-        for (uint32_t b = 0; b < CLASS_BUCKETS; ++b) {
-            base[b] = run;
+        for (uint32_t b = 0; b < tid; ++b)
             run += cc->count[b];
-        }
+        base[tid] = run;
     }
-    __syncthreads();
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nprimes; i += stride) {
-        const uint32_t code = codes[i];
-        if (code) {
-            const uint32_t b = class_bucket(code >> 16);
-            const uint32_t pos = base[b] + aggregated_increment(cc->fill, b);
-            items[pos] = ClassItem{primes[i], code, 0};
+    const uint64_t tile = (uint64_t)blockDim.x * REGROUP_PER_THREAD;
+    for (uint64_t t0 = (uint64_t)blockIdx.x * tile; t0 < nprimes; t0 += (uint64_t)gridDim.x * tile) {
+        if (tid < CLASS_BUCKETS)
+            hist[tid] = 0;
+        __syncthreads();
+        uint32_t code[REGROUP_PER_THREAD], off[REGROUP_PER_THREAD];
+#pragma unroll
+        for (int j = 0; j < REGROUP_PER_THREAD; ++j) {
+            const uint64_t i = t0 + (uint64_t)j * blockDim.x + tid;
+            code[j] = i < nprimes ? codes[i] : 0u;
+            if (code[j])
+                off[j] = aggregated_increment(hist, class_bucket(code[j] >> 16));
         }
+        __syncthreads();
+        if (tid < CLASS_BUCKETS)
+            tile_base[tid] = hist[tid] ? base[tid] + atomicAdd(&cc->fill[tid], hist[tid]) : 0u;
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < REGROUP_PER_THREAD; ++j) {
+            const uint64_t i = t0 + (uint64_t)j * blockDim.x + tid;
+            if (code[j])
+                items[tile_base[class_bucket(code[j] >> 16)] + off[j]] = ClassItem{primes[i], code[j], 0};
+        }
+        __syncthreads();
     }
 }
 
