@@ -197,33 +197,28 @@ CTD_HD bool quadratic_excluded(uint64_t p, uint64_t k, bool negate)
     return t == 0 || (two_qr && t < 0);
 }
 
-// A = 2^-e = 2^(p - 1 - e) (left-to-right, a set bit a doubling) and B =
-// wt^e = (-+1)^e k^e (left-to-right, Shoup multiplications by the plain k),
-// both in Montgomery form; 0 < e < p - 1, m with r2.
+// A = 2^-e = (1/2)^e and B = wt^e = (-+1)^e k^e, both in Montgomery form,
+// in one left-to-right loop over the bits of e: per bit a squaring of each,
+// and for a set bit a halving of A's Montgomery representative ((x R)/2 =
+// (x/2) R) and a Shoup multiplication of B by the plain k -- two
+// independent chains per iteration.  0 < e < p - 1, p < 2^63, m with r2.
 CTD_HD void power_pair(const Mont &m, uint64_t k, bool negate, uint64_t e, uint64_t &A, uint64_t &B)
 {
     const uint64_t p = m.p;
+    const uint64_t kr = k < p ? k : k % p;
+    const uint64_t ks = m.shoup(kr);
     A = m.one;
-    {
-        const uint64_t ea = p - 1 - e;
-        for (int b = 63 - clz64(ea); b >= 0; --b) {
-            A = m.mul(A, A);  // inline: the hot loops stay small
-            if ((ea >> b) & 1)
-                A = m.dbl(A);
-        }
-    }
     B = m.one;
-    {
-        const uint64_t kr = k < p ? k : k % p;
-        const uint64_t ks = m.shoup(kr);
-        for (int b = 63 - clz64(e); b >= 0; --b) {
-            B = m.mul(B, B);
-            if ((e >> b) & 1)
-                B = shoup_mul(B, kr, ks, p);
+    for (int b = 63 - clz64(e); b >= 0; --b) {
+        A = m.mul(A, A);  // inline: the hot loop stays small
+        B = m.mul(B, B);
+        if ((e >> b) & 1) {
+            A = (A + ((A & 1) ? p : 0)) >> 1;
+            B = shoup_mul(B, kr, ks, p);
         }
-        if (negate && (e & 1))
-            B = B ? p - B : 0;
     }
+    if (negate && (e & 1))
+        B = B ? p - B : 0;
 }
 
 // The class of the zeros of 2^-n = wt (mod p), wt = -k (negate) or k, for
