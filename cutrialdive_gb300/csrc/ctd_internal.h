@@ -115,6 +115,8 @@ struct ClassCounters {
     unsigned long long next;        // walk work counter
     uint32_t nrefine;               // primes listed for the rare-prime refinement
     uint32_t nlisted;               // primes the quadratic screen left for classification
+    uint32_t wide;                  // a prime of the launch is 2^40 or above
+    uint32_t pad;
 };
 // a prime with its class code (M << 16 | r)
 struct ClassItem {

@@ -64,17 +64,19 @@ CTD_HD void crt_merge_small(PowerClass &c, uint32_t j, uint32_t q)
 // Montgomery products inlined the kernel was large enough that warps
 // stalled on instruction fetch (ncu: "no instruction" the top stall).
 #ifdef __CUDA_ARCH__
+template <class MT>
 __device__ __noinline__ uint64_t powres_mul(uint64_t a, uint64_t b, uint64_t p, uint64_t pinv)
 {
-    Mont m;
+    MT m;
     m.p = p;
     m.pinv = pinv;
     return m.mul(a, b);
 }
 #else
+template <class MT>
 inline uint64_t powres_mul(uint64_t a, uint64_t b, uint64_t p, uint64_t pinv)
 {
-    Mont m;
+    MT m;
     m.p = p;
     m.pinv = pinv;
     return m.mul(a, b);
@@ -82,7 +84,8 @@ inline uint64_t powres_mul(uint64_t a, uint64_t b, uint64_t p, uint64_t pinv)
 #endif
 
 // base^e (base in Montgomery form, e small)
-CTD_HD uint64_t small_pow(const Mont &m, uint64_t base, uint32_t e)
+template <class MT>
+CTD_HD uint64_t small_pow(const MT &m, uint64_t base, uint32_t e)
 {
     uint64_t r = m.one;
     while (e) {
@@ -95,7 +98,8 @@ CTD_HD uint64_t small_pow(const Mont &m, uint64_t base, uint32_t e)
 }
 
 // x^(2^s)
-CTD_HD uint64_t square_n(const Mont &m, uint64_t x, int s)
+template <class MT>
+CTD_HD uint64_t square_n(const MT &m, uint64_t x, int s)
 {
     for (int i = 0; i < s; ++i)
         x = m.mul(x, x);
@@ -116,9 +120,10 @@ CTD_HD uint64_t shoup_mul(uint64_t x, uint64_t w, uint64_t ws, uint64_t p)
 struct Pow105 {
     uint64_t p15, p21, p35, p105;
 };
-CTD_HD Pow105 pow105(const Mont &m, uint64_t x)
+template <class MT>
+CTD_HD Pow105 pow105(const MT &m, uint64_t x)
 {
-    auto mul = [&](uint64_t a, uint64_t b) { return powres_mul(a, b, m.p, m.pinv); };
+    auto mul = [&](uint64_t a, uint64_t b) { return powres_mul<MT>(a, b, m.p, m.pinv); };
     const uint64_t x2 = mul(x, x), x3 = mul(x2, x), x5 = mul(x3, x2), x7 = mul(x5, x2);
     const uint64_t x10 = mul(x5, x5), x15 = mul(x10, x5), x14 = mul(x7, x7), x21 = mul(x14, x7);
     const uint64_t x35 = mul(x21, x14), x70 = mul(x35, x35), x105 = mul(x70, x35);
@@ -202,7 +207,8 @@ CTD_HD bool quadratic_excluded(uint64_t p, uint64_t k, bool negate)
 // and for a set bit a halving of A's Montgomery representative ((x R)/2 =
 // (x/2) R) and a Shoup multiplication of B by the plain k -- two
 // independent chains per iteration.  0 < e < p - 1, p < 2^63, m with r2.
-CTD_HD void power_pair(const Mont &m, uint64_t k, bool negate, uint64_t e, uint64_t &A, uint64_t &B)
+template <class MT>
+CTD_HD void power_pair(const MT &m, uint64_t k, bool negate, uint64_t e, uint64_t &A, uint64_t &B)
 {
     const uint64_t p = m.p;
     const uint64_t kr = k < p ? k : k % p;
@@ -226,7 +232,8 @@ CTD_HD void power_pair(const Mont &m, uint64_t k, bool negate, uint64_t e, uint6
 // initialised (r2 is needed for k's Shoup quotient).  The work is the same
 // for every prime -- two full powers, fixed chains, loops of fixed length
 // -- so the lanes of a warp stay together.
-CTD_HD PowerClass doubling_class(const Mont &m, uint64_t k, bool negate)
+template <class MT>
+CTD_HD PowerClass doubling_class(const MT &m, uint64_t k, bool negate)
 {
     const uint64_t p = m.p;
     const uint64_t p1 = p - 1;
@@ -242,7 +249,7 @@ CTD_HD PowerClass doubling_class(const Mont &m, uint64_t k, bool negate)
     e0 = f3 ? e0 / 3 : e0;
     e0 = f5 ? e0 / 5 : e0;
     e0 = f7 ? e0 / 7 : e0;
-    auto mul = [&](uint64_t a, uint64_t b) { return powres_mul(a, b, p, m.pinv); };
+    auto mul = [&](uint64_t a, uint64_t b) { return powres_mul<MT>(a, b, p, m.pinv); };
     uint64_t A, B;
     power_pair(m, k, negate, e0, A, B);
     // A and B lie in the D-th roots of unity.  For a q that does not divide
@@ -364,9 +371,10 @@ CTD_HD uint32_t rare_q_of(uint64_t p, uint32_t qmax)
 
 // j < q with z^j = y, for z of prime order q, 11 <= q <= 64 (baby steps
 // z^0 .. z^7, giant steps by z^-8 = z^(q - 8)); q when there is none
-CTD_HD uint32_t small_log(const Mont &m, uint64_t z, uint64_t y, uint32_t q)
+template <class MT>
+CTD_HD uint32_t small_log(const MT &m, uint64_t z, uint64_t y, uint32_t q)
 {
-    auto mul = [&](uint64_t a, uint64_t b) { return powres_mul(a, b, m.p, m.pinv); };
+    auto mul = [&](uint64_t a, uint64_t b) { return powres_mul<MT>(a, b, m.p, m.pinv); };
     uint64_t baby[8];
     baby[0] = m.one;
 #pragma unroll
@@ -389,7 +397,8 @@ CTD_HD uint32_t small_log(const Mont &m, uint64_t z, uint64_t y, uint32_t q)
 // character of q = rare_q_of(p, ...) (0: unchanged): with z = 2^-(p-1)/q
 // and y = wt^((p-1)/q), either z = 1 (no condition, or no zero at all when
 // y != 1) or n = log_z y (mod q).
-CTD_HD PowerClass refine_class(const Mont &m, uint64_t k, bool negate, PowerClass c, uint32_t q)
+template <class MT>
+CTD_HD PowerClass refine_class(const MT &m, uint64_t k, bool negate, PowerClass c, uint32_t q)
 {
     if (!c.M || !q)
         return c;

@@ -610,7 +610,7 @@ __device__ __forceinline__ uint64_t doubling_target(const JobView &job, uint64_t
 
 // code of a prime's class: M << 16 | r, 0 when p divides no term; primes of
 // 2^63 and above keep the plain walk (M = 1)
-template <uint32_t FAM>
+template <uint32_t FAM, class MT = Mont>
 __device__ __forceinline__ uint32_t doubling_class_code(const JobView &job, uint64_t p)
 {
     if (p >= (1ull << 63))
@@ -618,7 +618,7 @@ __device__ __forceinline__ uint32_t doubling_class_code(const JobView &job, uint
     const uint64_t k = FAM == MERSENNE ? 1 : (job.param < p ? job.param : job.param % p);
     if (!k)
         return 0;  // p | k: k 2^n -+ 1 = -+1 (mod p), never zero
-    Mont m;
+    MT m;
     m.init(p);
     const PowerClass c = doubling_class(m, k, FAM == PROTH);
     return c.M ? (c.M << 16) | c.r : 0u;
@@ -1629,11 +1629,11 @@ __device__ __forceinline__ bool wants_refine(const JobView &job, uint64_t p, uin
 }
 
 // the refined code of a classified prime (0: it divides no term)
-template <uint32_t FAM>
+template <uint32_t FAM, class MT>
 __device__ __forceinline__ uint32_t refined_code(const JobView &job, uint64_t p, uint32_t code)
 {
     const uint64_t k = FAM == MERSENNE ? 1 : (job.param < p ? job.param : job.param % p);
-    Mont m;
+    MT m;
     m.init(p);
     const PowerClass c = refine_class(m, k, FAM == PROTH, PowerClass{code >> 16, code & 0xffffu},
                                       rare_q_of(p, refine_qmax(job)));
@@ -1643,7 +1643,9 @@ __device__ __forceinline__ uint32_t refined_code(const JobView &job, uint64_t p,
 // The quadratic screen (Proth, Riesel): the primes whose target is a
 // quadratic non-residue while 2 is a residue (a quarter of them) divide no
 // term and get code 0 here; the others are listed for classify_kernel, so
-// its warps spend the two powers on primes that need them.
+// its warps spend the two powers on primes that need them.  Every family:
+// cc->wide is set when a prime is 2^40 or above (the class kernels then take
+// the general Montgomery product instead of the narrow one).
 template <uint32_t FAM>
 __global__ void __launch_bounds__(256) screen_kernel(JobView job, const uint64_t *__restrict__ primes,
                                                      uint64_t nprimes, uint32_t *__restrict__ codes,
@@ -1651,30 +1653,62 @@ __global__ void __launch_bounds__(256) screen_kernel(JobView job, const uint64_t
 {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nprimes; i += stride) {
-        if (quadratic_excluded(primes[i], job.param, FAM == PROTH))
+        const uint64_t p = primes[i];
+        if (p >= MONT_NARROW_LIMIT)
+            cc->wide = 1;
+        if (!listed)
+            continue;
+        if (quadratic_excluded(p, job.param, FAM == PROTH))
             codes[i] = 0;
         else
             listed[aggregated_increment(&cc->nlisted, 0)] = (uint32_t)i;
     }
 }
 
-// the classes of the listed primes (all primes when `listed` is null)
+template <uint32_t FAM, class MT>
+__device__ __forceinline__ void classify_range(const JobView &job, const uint64_t *__restrict__ primes, uint64_t n,
+                                               uint32_t *__restrict__ codes, ClassCounters *__restrict__ cc,
+                                               uint32_t *__restrict__ refine, const uint32_t *__restrict__ listed)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+        const uint64_t i = listed ? listed[t] : t;
+        const uint64_t p = primes[i];
+        const uint32_t code = doubling_class_code<FAM, MT>(job, p);
+        codes[i] = code;
+        if (wants_refine(job, p, code))
+            refine[aggregated_increment(&cc->nrefine, 0)] = (uint32_t)i;
+        else if (code)
+            aggregated_increment(cc->count, class_bucket(code >> 16));
+    }
+}
+
+// the classes of the listed primes (all primes when `listed` is null), by
+// the narrow Montgomery product unless the screen saw a prime of 2^40 or more
 template <uint32_t FAM>
 __global__ void __launch_bounds__(256, 4) classify_kernel(JobView job, const uint64_t *__restrict__ primes,
                                                        uint64_t nprimes, uint32_t *__restrict__ codes,
                                                        ClassCounters *__restrict__ cc, uint32_t *__restrict__ refine,
                                                        const uint32_t *__restrict__ listed)
 {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     const uint64_t n = listed ? cc->nlisted : nprimes;
-    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
-        const uint64_t i = listed ? listed[t] : t;
-        const uint64_t p = primes[i];
-        const uint32_t code = doubling_class_code<FAM>(job, p);
+    if (cc->wide)
+        classify_range<FAM, Mont>(job, primes, n, codes, cc, refine, listed);
+    else
+        classify_range<FAM, MontN>(job, primes, n, codes, cc, refine, listed);
+}
+
+template <uint32_t FAM, class MT>
+__device__ __forceinline__ void refine_range(const JobView &job, const uint64_t *__restrict__ primes,
+                                             uint32_t *__restrict__ codes, ClassCounters *__restrict__ cc,
+                                             const uint32_t *__restrict__ refine, uint32_t n)
+{
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+        const uint32_t i = refine[t];
+        const uint32_t code = refined_code<FAM, MT>(job, primes[i], codes[i]);
         codes[i] = code;
-        if (wants_refine(job, p, code))
-            refine[aggregated_increment(&cc->nrefine, 0)] = (uint32_t)i;
-        else if (code)
+        if (code)
             aggregated_increment(cc->count, class_bucket(code >> 16));
     }
 }
@@ -1686,15 +1720,10 @@ __global__ void __launch_bounds__(256) refine_kernel(JobView job, const uint64_t
                                                      uint32_t *__restrict__ codes, ClassCounters *__restrict__ cc,
                                                      const uint32_t *__restrict__ refine)
 {
-    const uint32_t n = cc->nrefine;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
-        const uint32_t i = refine[t];
-        const uint32_t code = refined_code<FAM>(job, primes[i], codes[i]);
-        codes[i] = code;
-        if (code)
-            aggregated_increment(cc->count, class_bucket(code >> 16));
-    }
+    if (cc->wide)
+        refine_range<FAM, Mont>(job, primes, codes, cc, refine, cc->nrefine);
+    else
+        refine_range<FAM, MontN>(job, primes, codes, cc, refine, cc->nrefine);
 }
 
 // Each CTA regroups tiles of 256 x REGROUP_PER_THREAD primes: a histogram of
@@ -2303,9 +2332,10 @@ static int launch_classified(const JobView &v, const uint64_t *d_primes, uint64_
     cudaError_t e = cudaMemsetAsync(rs->counters, 0, sizeof(ClassCounters), st);
     const uint64_t want = (n + 255) / 256;
     const int cgrid = (int)(want < (uint64_t)rs->sm_count * 8 ? want : (uint64_t)rs->sm_count * 8);
-    // the quadratic screen (Mersenne's target 1 is always a residue)
+    // the quadratic screen (Mersenne's target 1 is always a residue: its
+    // pass only looks for primes of 2^40 and above)
     uint32_t *listed = FAM == MERSENNE ? nullptr : rs->listed;
-    if (e == cudaSuccess && listed) {
+    if (e == cudaSuccess) {
         screen_kernel<FAM><<<cgrid, 256, 0, st>>>(v, d_primes, n, rs->codes, rs->counters, listed);
         e = cudaGetLastError();
         if (e == cudaSuccess)

@@ -2,7 +2,9 @@
 // __host__ __device__, so the same source runs on the CPU here).  Reads
 // "p e k" lines on stdin, prints "one r2 pow2 kpow2 tok mu shoup" per line:
 // R mod p, R^2 mod p, 2^e mod p, k*2^e mod p (Montgomery form times plain k),
-// from(to(k)) for R = 2^64, floor(2^64 / p) and floor((k mod p) 2^64 / p).
+// from(to(k)) for R = 2^64, floor(2^64 / p) and floor((k mod p) 2^64 / p);
+// then, for p < 2^40 (0 0 otherwise), 2^e mod p and (k mod p)(k/2^7 mod p)
+// R^-1 mod p through the narrow Montgomery product.
 #include <cinttypes>
 #include <cstdio>
 
@@ -16,8 +18,16 @@ int main()
         m.init(p);
         const uint64_t U = m.pow2(e);
         const uint64_t kk = k < p ? k : k % p;
-        std::printf("%" PRIu64 " %" PRIu64 " %" PRIu64 " %" PRIu64 " %" PRIu64 " %" PRIu64 " %" PRIu64 "\n", m.one,
-                    m.r2, m.from(U), m.mul(U, kk), m.from(m.to(k)), m.mu(), m.shoup(kk));
+        uint64_t npow = 0, nmul = 0;
+        if (p < ctd::MONT_NARROW_LIMIT) {
+            ctd::MontN n;
+            n.init(p);
+            npow = n.from(n.pow2(e));
+            nmul = n.mul(kk, (k >> 7) % p);
+        }
+        std::printf("%" PRIu64 " %" PRIu64 " %" PRIu64 " %" PRIu64 " %" PRIu64 " %" PRIu64 " %" PRIu64 " %" PRIu64
+                    " %" PRIu64 "\n",
+                    m.one, m.r2, m.from(U), m.mul(U, kk), m.from(m.to(k)), m.mu(), m.shoup(kk), npow, nmul);
     }
     return 0;
 }

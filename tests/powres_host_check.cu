@@ -4,7 +4,8 @@
 // 2^-n = wt (mod p) satisfies n = r (mod M), and n = r2 (mod M2) after the
 // refinement by the smallest rare prime q = 11 .. 61 dividing p - 1; M = 0 (M2 = 0)
 // when no n does; then "x" (1 when the quadratic screen excludes p) and the
-// Jacobi symbol (wt/p).
+// Jacobi symbol (wt/p); last 1 when the classes through the narrow
+// Montgomery product (p < 2^40) equal these (always 1 above 2^40).
 #include <cinttypes>
 #include <cstdio>
 
@@ -20,7 +21,15 @@ int main()
         const ctd::PowerClass c = ctd::doubling_class(m, p - wt, true);
         const ctd::PowerClass f = ctd::refine_class(m, p - wt, true, c, ctd::rare_q_of(p, 61));
         const int x = ctd::quadratic_excluded(p, p - wt, true) ? 1 : 0;
-        std::printf("%u %u %u %u %d %d\n", c.M, c.r, f.M, f.r, x, ctd::jacobi(wt, p));
+        int same = 1;
+        if (p < ctd::MONT_NARROW_LIMIT) {
+            ctd::MontN n;
+            n.init(p);
+            const ctd::PowerClass cn = ctd::doubling_class(n, p - wt, true);
+            const ctd::PowerClass fn = ctd::refine_class(n, p - wt, true, cn, ctd::rare_q_of(p, 61));
+            same = cn.M == c.M && cn.r == c.r && fn.M == f.M && fn.r == f.r;
+        }
+        std::printf("%u %u %u %u %d %d %d\n", c.M, c.r, f.M, f.r, x, ctd::jacobi(wt, p), same);
     }
     return 0;
 }

@@ -28,7 +28,7 @@ def cases():
     rnd = random.Random(5)
     out = [(3, 0, 1), (3, 1, 2), (5, 64, 7), (2**61 - 1, 100000, 3), (2**64 - 59, 12345, 2**64 - 1),
            (2**63 + 29, 1, 999999), ((1 << 32) + 15, 99999, 3)]
-    for bits in (8, 20, 31, 32, 33, 40, 50, 62, 63, 64):
+    for bits in (8, 20, 31, 32, 33, 34, 35, 36, 38, 39, 40, 50, 62, 63, 64):
         for _ in range(25):
             p = rnd.getrandbits(bits) | 1 | (1 << (bits - 1))
             if p < 3:
@@ -43,7 +43,7 @@ def test_montgomery_setup_and_pow2(checker):
     res = subprocess.run([checker], input=inp, capture_output=True, text=True, check=True).stdout.split("\n")
     R = 1 << 64
     for (p, e, k), line in zip(cs, res):
-        one, r2, pw, kpw, tok, mu, sh = map(int, line.split())
+        one, r2, pw, kpw, tok, mu, sh, npw, nmul = map(int, line.split())
         assert one == R % p, (p, e)
         assert r2 == R * R % p, (p, e)
         assert pw == pow(2, e, p), (p, e)
@@ -51,6 +51,9 @@ def test_montgomery_setup_and_pow2(checker):
         assert tok == k % p, (p, k)
         assert mu == R // p, p
         assert sh == (k % p) * R // p, (p, k)
+        if p < 1 << 40:  # the narrow Montgomery product
+            assert npw == pow(2, e, p), (p, e)
+            assert nmul == (k % p) * ((k >> 7) % p) * pow(R, -1, p) % p, (p, k)
 
 
 def smarandache_mod(b: int, s: int, p: int) -> int:

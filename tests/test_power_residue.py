@@ -35,7 +35,8 @@ def classes(checker, cases):
 
 def both(got):
     """(M, r) of the base class and of the refined one, for each case"""
-    return [((M, r), (M2, r2)) for M, r, M2, r2, _, _ in got]
+    assert all(g[6] == 1 for g in got), "narrow Montgomery classes differ"
+    return [((M, r), (M2, r2)) for M, r, M2, r2, _, _, _ in got]
 
 
 def test_quadratic_screen_and_jacobi(checker):
@@ -50,7 +51,8 @@ def test_quadratic_screen_and_jacobi(checker):
     cases += [(p, w) for p in map(int, sympy.primerange(3, 200)) for w in range(1, p)]
     got = classes(checker, cases)
     screened = 0
-    for (p, w), (M, _, M2, _, x, jac) in zip(cases, got):
+    assert all(g[6] == 1 for g in got), "narrow Montgomery classes differ"
+    for (p, w), (M, _, M2, _, x, jac, _) in zip(cases, got):
         assert jac == sympy.jacobi_symbol(w, p), (p, w, jac)
         if x:
             screened += 1
