@@ -81,10 +81,11 @@ PLAIN = {
 FAMILY_NAMES = {0: "MERSENNE", 1: "PROTH", 2: "RIESEL", 3: "SMARANDACHE", 4: "FIBONACCI", 5: "LUCAS",
                 6: "PROTH_FIXED_N", 7: "RIESEL_FIXED_N", 8: "TRIBONACCI"}
 # Roofline inputs per workload (what the dominant launch executes):
-#  * proth -- the classified doubling launch (classify_kernel, refine_kernel,
-#    regroup_kernel, class_walk_kernel): bound by integer issue slots.
-#    Thread instructions and DRAM bytes per prime come from one ncu capture of
-#    the same four kernels on the 2^27-wide segment [2^32, 2^32 + 2^27) of this workload
+#  * proth -- the classified doubling launch (screen_kernel, classify_kernel,
+#    refine_kernel, regroup_kernel, class_walk_kernel): bound by integer
+#    issue slots.  Thread instructions and DRAM bytes per prime come from one
+#    ncu capture of the same five kernels on the 2^27-wide segment
+#    [2^32, 2^32 + 2^27) of this workload
 #    (6,047,768 primes; the capture's command is in the profile summary);
 #    the live launch time comes from CUDA events in this run.
 #  * smarandache -- the 32-bit Shoup step (p < 2^30): three 32-bit
@@ -95,10 +96,11 @@ FAMILY_NAMES = {0: "MERSENNE", 1: "PROTH", 2: "RIESEL", 3: "SMARANDACHE", 4: "FI
 #    shifts per block = 57/18 ALU operations per update, against the ALU
 #    compare rate measured now.
 PROTH_NCU = {"primes": 6047768,
-             "thread_inst": {"classify_kernel": 1754494365 * 23.49, "refine_kernel": 332382689 * 24.78,
-                             "regroup_kernel": 29143348 * 17.15, "class_walk_kernel": 2306859367 * 29.82},
-             "dram_bytes": (48.430848 + 1.414912 + 78.400256 + 1.527808 + 72.644096 + 12.022784 + 54.270976
-                            + 7.208704) * 1e6}
+             "thread_inst": {"screen_kernel": 56524200 * 30.87, "classify_kernel": 1193287874 * 25.31,
+                             "refine_kernel": 301277230 * 24.99, "regroup_kernel": 53971012 * 16.98,
+                             "class_walk_kernel": 2108416057 * 29.62},
+             "dram_bytes": (59.566336 + 12.364544 + 76.983808 + 13.673984 + 78.414592 + 1.666560 + 72.933632
+                            + 12.878336 + 54.180864 + 7.825920) * 1e6}
 SMARANDACHE_MULS_PER_UPDATE = 3
 TRIBONACCI_ALU_OPS_PER_UPDATE = 57 / 18
 
@@ -436,11 +438,12 @@ def run_ours(args, world, rank, local):
         achieved = inst / launch_s
         roofline = {
             "bound": "int_issue",
-            "kernel": "classify_kernel<PROTH> + refine_kernel<PROTH> + regroup_kernel + class_walk_kernel<PROTH>",
+            "kernel": "screen_kernel<PROTH> + classify_kernel<PROTH> + refine_kernel<PROTH> + regroup_kernel + "
+                      "class_walk_kernel<PROTH>",
             "achieved": achieved / 1e9, "peak": (peaks["int"] / 1e9) if peaks["int"] else None, "unit": "Ginst/s",
             "frac": (achieved / peaks["int"]) if peaks["int"] else None,
             "thread_instructions_per_update": inst / per_launch_updates, "launch_ms": launch_s * 1e3,
-            "achieved_source": "ncu thread instructions of the four kernels on a 2^27-segment of this workload, "
+            "achieved_source": "ncu thread instructions of the five kernels on a 2^27-segment of this workload, "
                                "scaled by the primes per launch, over the CUDA-event launch time of this run",
             "peak_source": "measured now: libctd_probe add/xor chains (integer issue rate) on this GPU",
             "traffic": PROTH_NCU["dram_bytes"] / PROTH_NCU["primes"] * primes_launch,
