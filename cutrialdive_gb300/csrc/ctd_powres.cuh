@@ -215,14 +215,18 @@ CTD_HD void power_pair(const MT &m, uint64_t k, bool negate, uint64_t e, uint64_
     const uint64_t ks = m.shoup(kr);
     A = m.one;
     B = m.one;
+    // A and B stay below 2p (the narrow product's lazy form; a halving of
+    // x < 2p is below 1.5p; Shoup's product of x < 2^64 is below p)
     for (int b = 63 - clz64(e); b >= 0; --b) {
-        A = m.mul(A, A);  // inline: the hot loop stays small
-        B = m.mul(B, B);
+        A = m.mul_lazy(A, A);  // inline: the hot loop stays small
+        B = m.mul_lazy(B, B);
         if ((e >> b) & 1) {
             A = (A + ((A & 1) ? p : 0)) >> 1;
             B = shoup_mul(B, kr, ks, p);
         }
     }
+    A = m.canon(A);
+    B = m.canon(B);
     if (negate && (e & 1))
         B = B ? p - B : 0;
 }
