@@ -190,6 +190,7 @@ struct BatchCache {
         s.ctl = ctl;
         s.codes = codes;
         s.items = items;
+        s.class_cap = std::min<uint64_t>(codes_cap, items_cap);
         s.bucket_count = bucket;
         s.bucket_base = bucket + 2ull * nactive * CLASS_BUCKETS;
         return s;
@@ -407,6 +408,8 @@ int ctd_batch_run(ctd_ctx *ctx, const ctd_job *jobs, uint32_t njobs, uint32_t *c
                               (const void *)bc.codes, (const void *)bc.items, (const void *)bc.bucket})
             h.add(p);
         h.add(bc.primes_cap);
+        h.add(bc.codes_cap);  // the pair lists sit in the items buffer at class_cap
+        h.add(bc.items_cap);
         for (uint32_t i = 0; i < njobs; ++i)
             if (jobs[i].f0 <= 2 && jobs[i].f1 > 2)
                 h.add(hjobs[i].view);
@@ -834,6 +837,7 @@ int ctd_serve_tick(ctd_server *srv, uint64_t *done_ids, uint32_t cap, uint32_t *
                 bs.ctl = srv->d_ctl;
                 bs.codes = srv->d_codes;
                 bs.items = srv->d_items;
+                bs.class_cap = srv->class_cap;
                 bs.bucket_count = srv->d_bucket;
                 bs.bucket_base = srv->d_bucket + 2ull * (used - first) * CLASS_BUCKETS;
                 rc = launch_batch(srv->d_jobs, d_act + first, gcount, any_cls, srv->d_primes, d_count, lo, hi,

@@ -186,16 +186,21 @@ struct BatchControl {
     uint64_t nclass;                        // (classified job, prime) pairs
     uint64_t total_warps[BATCH_GROUPS];     // warp items of each group's walk
     unsigned long long next[BATCH_GROUPS];  // the walks' work counters
+    unsigned long long nlisted;             // pairs the quadratic screen left for classification
+    unsigned long long nrefine;             // pairs listed for the rare-prime refinement
 };
 // Device scratch of one batched segment (sized by the caller):
 // spans[nactive + 1], codes/items[class pairs], bucket_count[2 * nactive *
 // CLASS_BUCKETS] (counts, then regroup cursors), bucket_base[nactive *
-// CLASS_BUCKETS].
+// CLASS_BUCKETS].  The screen's and the refinement's pair lists (8 bytes a
+// pair each) live in the items buffer (16 bytes a pair), which holds nothing
+// until the regroup that follows them.
 struct BatchScratch {
     BatchSpan *spans;
     BatchControl *ctl;
     uint32_t *codes;
     ClassItem *items;
+    uint64_t class_cap;  // pairs the codes and items buffers hold
     uint32_t *bucket_count;
     uint32_t *bucket_base;
 };

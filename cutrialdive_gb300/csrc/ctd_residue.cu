@@ -1834,8 +1834,11 @@ static cudaError_t allow_smem(K kernel, size_t bytes)
 //   batch_bounds_kernel   each active job's sub-range of the sorted primes,
 //                         and for the classified (doubling) jobs their
 //                         offsets in the class buffers;
-//   batch_classify_kernel power-residue class of every (classified job,
-//                         prime) pair, counted per job and class;
+//   batch_screen_kernel, batch_classify_kernel, batch_refine_kernel
+//                         power-residue class of every (classified job,
+//                         prime) pair, as in the plain launch (screen,
+//                         classes, rare-prime refinement), counted per job
+//                         and class;
 //   batch_plan_kernel     per job: class bases, its (prime, tile) units and
 //                         the exclusive prefix of warp items over the jobs;
 //   batch_regroup_kernel  the classified pairs written class by class;
@@ -1906,6 +1909,8 @@ __global__ void __launch_bounds__(1024) batch_bounds_kernel(BatchJob *__restrict
         }
         spans[nactive].coff = run;
         ctl->nclass = run;
+        ctl->nlisted = 0;
+        ctl->nrefine = 0;
     }
 }
 
@@ -1915,13 +1920,58 @@ __device__ __forceinline__ uint32_t class_job(const BatchSpan *spans, uint32_t n
     return last_le(nactive, t, [&](uint32_t i) { return spans[i].coff; });
 }
 
-__global__ void __launch_bounds__(256) batch_classify_kernel(const BatchJob *__restrict__ jobs,
-                                                             const uint32_t *__restrict__ active, uint32_t nactive,
-                                                             const uint64_t *__restrict__ primes,
-                                                             const BatchSpan *__restrict__ spans,
-                                                             const BatchControl *__restrict__ ctl,
-                                                             uint32_t *__restrict__ codes,
-                                                             uint32_t *__restrict__ bucket_count)
+// warp-aggregated atomicAdd of 1 per active lane on a 64-bit counter;
+// returns this lane's old value
+__device__ __forceinline__ unsigned long long aggregated_append(unsigned long long *counter)
+{
+    const uint32_t act = __activemask();
+    const int leader = __ffs(act) - 1;
+    const uint32_t lane = threadIdx.x & 31u;
+    unsigned long long base = 0;
+    if ((int)lane == leader)
+        base = atomicAdd(counter, (unsigned long long)__popc(act));
+    base = __shfl_sync(act, base, leader);
+    return base + (unsigned long long)__popc(act & ((1u << lane) - 1u));
+}
+
+// the class code of a prime for a job of any doubling family (the family
+// read at run time: one copy of the classification per product)
+template <class MT>
+__device__ __forceinline__ uint32_t class_code_rt(const JobView &v, uint64_t p)
+{
+    if (p >= (1ull << 63))
+        return 1u << 16;
+    const uint64_t k = v.family == MERSENNE ? 1 : (v.param < p ? v.param : v.param % p);
+    if (!k)
+        return 0;
+    MT m;
+    m.init(p);
+    const PowerClass c = doubling_class(m, k, v.family == PROTH);
+    return c.M ? (c.M << 16) | c.r : 0u;
+}
+template <class MT>
+__device__ __forceinline__ uint32_t refined_code_rt(const JobView &v, uint64_t p, uint32_t code)
+{
+    const uint64_t k = v.family == MERSENNE ? 1 : (v.param < p ? v.param : v.param % p);
+    MT m;
+    m.init(p);
+    const PowerClass c = refine_class(m, k, v.family == PROTH, PowerClass{code >> 16, code & 0xffffu},
+                                      rare_q_of(p, refine_qmax(v)));
+    return c.M ? (c.M << 16) | c.r : 0u;
+}
+
+// The batched forms of screen_kernel, classify_kernel and refine_kernel
+// over the segment's (classified job, prime) pairs t: the screen lists the
+// pairs it does not exclude, classification lists the pairs with a rare q,
+// the refinement narrows them; the pairs with a class are counted per job
+// and class.  Lists of pair numbers in the items buffer (free until the
+// regroup).  Primes below 2^40 multiply with the narrow product.
+__global__ void __launch_bounds__(256) batch_screen_kernel(const BatchJob *__restrict__ jobs,
+                                                           const uint32_t *__restrict__ active, uint32_t nactive,
+                                                           const uint64_t *__restrict__ primes,
+                                                           const BatchSpan *__restrict__ spans,
+                                                           BatchControl *__restrict__ ctl,
+                                                           uint32_t *__restrict__ codes, uint64_t *__restrict__ listed)
 {
     const uint64_t total = ctl->nclass;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -1929,9 +1979,57 @@ __global__ void __launch_bounds__(256) batch_classify_kernel(const BatchJob *__r
         const uint32_t i = class_job(spans, nactive, t);
         const JobView &v = jobs[active[i]].view;
         const uint64_t p = primes[spans[i].pbeg + (t - spans[i].coff)];
-        const uint32_t code = v.family == PROTH    ? doubling_class_code<PROTH>(v, p)
-                              : v.family == RIESEL ? doubling_class_code<RIESEL>(v, p)
-                                                   : doubling_class_code<MERSENNE>(v, p);
+        if (v.family != MERSENNE && quadratic_excluded(p, v.param, v.family == PROTH))
+            codes[t] = 0;
+        else
+            listed[aggregated_append(&ctl->nlisted)] = t;
+    }
+}
+
+__global__ void __launch_bounds__(256, 4) batch_classify_kernel(const BatchJob *__restrict__ jobs,
+                                                                const uint32_t *__restrict__ active, uint32_t nactive,
+                                                                const uint64_t *__restrict__ primes,
+                                                                const BatchSpan *__restrict__ spans,
+                                                                BatchControl *__restrict__ ctl,
+                                                                uint32_t *__restrict__ codes,
+                                                                uint32_t *__restrict__ bucket_count,
+                                                                const uint64_t *__restrict__ listed,
+                                                                uint64_t *__restrict__ refine)
+{
+    const uint64_t total = ctl->nlisted;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += stride) {
+        const uint64_t t = listed[x];
+        const uint32_t i = class_job(spans, nactive, t);
+        const JobView &v = jobs[active[i]].view;
+        const uint64_t p = primes[spans[i].pbeg + (t - spans[i].coff)];
+        const uint32_t code = p < MONT_NARROW_LIMIT ? class_code_rt<MontN>(v, p) : class_code_rt<Mont>(v, p);
+        codes[t] = code;
+        if (wants_refine(v, p, code))
+            refine[aggregated_append(&ctl->nrefine)] = t;
+        else if (code)
+            aggregated_increment(bucket_count, i * CLASS_BUCKETS + class_bucket(code >> 16));
+    }
+}
+
+__global__ void __launch_bounds__(256) batch_refine_kernel(const BatchJob *__restrict__ jobs,
+                                                           const uint32_t *__restrict__ active, uint32_t nactive,
+                                                           const uint64_t *__restrict__ primes,
+                                                           const BatchSpan *__restrict__ spans,
+                                                           const BatchControl *__restrict__ ctl,
+                                                           uint32_t *__restrict__ codes,
+                                                           uint32_t *__restrict__ bucket_count,
+                                                           const uint64_t *__restrict__ refine)
+{
+    const uint64_t total = ctl->nrefine;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += stride) {
+        const uint64_t t = refine[x];
+        const uint32_t i = class_job(spans, nactive, t);
+        const JobView &v = jobs[active[i]].view;
+        const uint64_t p = primes[spans[i].pbeg + (t - spans[i].coff)];
+        const uint32_t code = p < MONT_NARROW_LIMIT ? refined_code_rt<MontN>(v, p, codes[t])
+                                                    : refined_code_rt<Mont>(v, p, codes[t]);
         codes[t] = code;
         if (code)
             aggregated_increment(bucket_count, i * CLASS_BUCKETS + class_bucket(code >> 16));
@@ -1981,6 +2079,10 @@ __global__ void __launch_bounds__(1024) batch_plan_kernel(const BatchJob *__rest
     }
 }
 
+// Tiles of 256 x REGROUP_PER_THREAD pairs: a tile inside one job (the
+// usual case: a job's pairs are consecutive) takes a shared-memory
+// histogram and one global atomic per class, as regroup_kernel does; a tile
+// across jobs takes one global atomic per (job, class) and warp.
 __global__ void __launch_bounds__(256) batch_regroup_kernel(const uint32_t *__restrict__ active, uint32_t nactive,
                                                             const uint64_t *__restrict__ primes,
                                                             const BatchSpan *__restrict__ spans,
@@ -1990,16 +2092,52 @@ __global__ void __launch_bounds__(256) batch_regroup_kernel(const uint32_t *__re
                                                             uint32_t *__restrict__ bucket_fill,
                                                             ClassItem *__restrict__ items)
 {
+    __shared__ uint32_t hist[CLASS_BUCKETS];
+    __shared__ uint32_t tile_base[CLASS_BUCKETS];
+    const uint32_t tid = threadIdx.x;
     const uint64_t total = ctl->nclass;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
-        const uint32_t code = codes[t];
-        if (!code)
-            continue;
-        const uint32_t i = class_job(spans, nactive, t);
-        const uint32_t key = i * CLASS_BUCKETS + class_bucket(code >> 16);
-        const uint64_t pos = spans[i].coff + bucket_base[key] + aggregated_increment(bucket_fill, key);
-        items[pos] = ClassItem{primes[spans[i].pbeg + (t - spans[i].coff)], code, 0};
+    const uint64_t tile = (uint64_t)blockDim.x * REGROUP_PER_THREAD;
+    for (uint64_t t0 = (uint64_t)blockIdx.x * tile; t0 < total; t0 += (uint64_t)gridDim.x * tile) {
+        const uint64_t t1 = t0 + tile < total ? t0 + tile : total;
+        const uint32_t i0 = class_job(spans, nactive, t0);
+        if (class_job(spans, nactive, t1 - 1) != i0) {
+            for (uint64_t t = t0 + tid; t < t1; t += blockDim.x) {
+                const uint32_t code = codes[t];
+                if (!code)
+                    continue;
+                const uint32_t i = class_job(spans, nactive, t);
+                const uint32_t key = i * CLASS_BUCKETS + class_bucket(code >> 16);
+                const uint64_t pos = spans[i].coff + bucket_base[key] + aggregated_increment(bucket_fill, key);
+                items[pos] = ClassItem{primes[spans[i].pbeg + (t - spans[i].coff)], code, 0};
+            }
+            continue;  // uniform over the CTA: no barrier skipped unevenly
+        }
+        if (tid < CLASS_BUCKETS)
+            hist[tid] = 0;
+        __syncthreads();
+        uint32_t code[REGROUP_PER_THREAD], off[REGROUP_PER_THREAD];
+#pragma unroll
+        for (int j = 0; j < REGROUP_PER_THREAD; ++j) {
+            const uint64_t t = t0 + (uint64_t)j * blockDim.x + tid;
+            code[j] = t < t1 ? codes[t] : 0u;
+            if (code[j])
+                off[j] = aggregated_increment(hist, class_bucket(code[j] >> 16));
+        }
+        __syncthreads();
+        if (tid < CLASS_BUCKETS)
+            tile_base[tid] = hist[tid] ? bucket_base[i0 * CLASS_BUCKETS + tid] +
+                                             atomicAdd(&bucket_fill[i0 * CLASS_BUCKETS + tid], hist[tid])
+                                       : 0u;
+        __syncthreads();
+        const BatchSpan sp = spans[i0];
+#pragma unroll
+        for (int j = 0; j < REGROUP_PER_THREAD; ++j) {
+            const uint64_t t = t0 + (uint64_t)j * blockDim.x + tid;
+            if (code[j])
+                items[sp.coff + tile_base[class_bucket(code[j] >> 16)] + off[j]] =
+                    ClassItem{primes[sp.pbeg + (t - sp.coff)], code[j], 0};
+        }
+        __syncthreads();
     }
 }
 
@@ -2122,10 +2260,25 @@ int launch_batch(BatchJob *d_jobs, const uint32_t *d_active, const uint32_t gcou
         note_kernel_launch();
     }
     if (rc == cudaSuccess && any_classified) {
-        batch_classify_kernel<<<cgrid, 256, 0, st>>>(d_jobs, d_active, nactive, d_primes, bs.spans, bs.ctl,
-                                                     bs.codes, bs.bucket_count);
+        // the pair lists in the items buffer: [0, class_cap) and [class_cap, 2 class_cap) words
+        uint64_t *listed = reinterpret_cast<uint64_t *>(bs.items);
+        uint64_t *refine = listed + bs.class_cap;
+        batch_screen_kernel<<<cgrid, 256, 0, st>>>(d_jobs, d_active, nactive, d_primes, bs.spans, bs.ctl, bs.codes,
+                                                   listed);
         rc = cudaGetLastError();
         note_kernel_launch();
+        if (rc == cudaSuccess) {
+            batch_classify_kernel<<<cgrid, 256, 0, st>>>(d_jobs, d_active, nactive, d_primes, bs.spans, bs.ctl,
+                                                         bs.codes, bs.bucket_count, listed, refine);
+            rc = cudaGetLastError();
+            note_kernel_launch();
+        }
+        if (rc == cudaSuccess) {
+            batch_refine_kernel<<<cgrid, 256, 0, st>>>(d_jobs, d_active, nactive, d_primes, bs.spans, bs.ctl,
+                                                       bs.codes, bs.bucket_count, refine);
+            rc = cudaGetLastError();
+            note_kernel_launch();
+        }
     }
     if (rc == cudaSuccess) {
         batch_plan_kernel<<<1, 1024, 0, st>>>(d_jobs, d_active, nactive, bs.spans, bs.ctl, bs.bucket_count,
