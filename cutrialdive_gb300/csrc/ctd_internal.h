@@ -116,7 +116,7 @@ struct ClassCounters {
     uint32_t nrefine;               // primes listed for the rare-prime refinement
     uint32_t nlisted;               // primes the quadratic screen left for classification
     uint32_t wide;                  // a prime of the launch is 2^40 or above
-    uint32_t pad;
+    uint32_t nnine;                 // primes listed for the 9th-power character
 };
 // a prime with its class code (M << 16 | r)
 struct ClassItem {
@@ -131,6 +131,7 @@ struct ResidueScratch {
     ClassItem *items = nullptr;
     uint32_t *refine = nullptr;  // indices of the primes to refine
     uint32_t *listed = nullptr;  // indices of the primes to classify
+    uint32_t *nine = nullptr;    // indices of the primes for the 9th-power character
     uint64_t cap = 0;  // primes
     ClassCounters *counters = nullptr;
 };

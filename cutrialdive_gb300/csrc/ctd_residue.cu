@@ -1628,6 +1628,23 @@ __device__ __forceinline__ bool wants_refine(const JobView &job, uint64_t p, uin
     return code && p < (1ull << 63) && rare_q_of(p, refine_qmax(job)) != 0;
 }
 
+// whether a classified prime goes to the 9th-power character's pass
+__device__ __forceinline__ bool wants_nine(const JobView &job, uint64_t p, uint32_t code)
+{
+    return code && p < (1ull << 63) && refine_qmax(job) >= 11 && (p - 1) % 9 == 0;
+}
+
+// the code of a classified prime narrowed by the 9th-power character
+template <uint32_t FAM, class MT>
+__device__ __forceinline__ uint32_t nine_code(const JobView &job, uint64_t p, uint32_t code)
+{
+    const uint64_t k = FAM == MERSENNE ? 1 : (job.param < p ? job.param : job.param % p);
+    MT m;
+    m.init(p);
+    const PowerClass c = nine_class(m, k, FAM == PROTH, PowerClass{code >> 16, code & 0xffffu});
+    return c.M ? (c.M << 16) | c.r : 0u;
+}
+
 // the refined code of a classified prime (0: it divides no term)
 template <uint32_t FAM, class MT>
 __device__ __forceinline__ uint32_t refined_code(const JobView &job, uint64_t p, uint32_t code)
@@ -1668,7 +1685,8 @@ __global__ void __launch_bounds__(256) screen_kernel(JobView job, const uint64_t
 template <uint32_t FAM, class MT>
 __device__ __forceinline__ void classify_range(const JobView &job, const uint64_t *__restrict__ primes, uint64_t n,
                                                uint32_t *__restrict__ codes, ClassCounters *__restrict__ cc,
-                                               uint32_t *__restrict__ refine, const uint32_t *__restrict__ listed)
+                                               uint32_t *__restrict__ refine, uint32_t *__restrict__ nine,
+                                               const uint32_t *__restrict__ listed)
 {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
@@ -1678,6 +1696,8 @@ __device__ __forceinline__ void classify_range(const JobView &job, const uint64_
         codes[i] = code;
         if (wants_refine(job, p, code))
             refine[aggregated_increment(&cc->nrefine, 0)] = (uint32_t)i;
+        else if (wants_nine(job, p, code))
+            nine[aggregated_increment(&cc->nnine, 0)] = (uint32_t)i;
         else if (code)
             aggregated_increment(cc->count, class_bucket(code >> 16));
     }
@@ -1689,26 +1709,30 @@ template <uint32_t FAM>
 __global__ void __launch_bounds__(256, 4) classify_kernel(JobView job, const uint64_t *__restrict__ primes,
                                                        uint64_t nprimes, uint32_t *__restrict__ codes,
                                                        ClassCounters *__restrict__ cc, uint32_t *__restrict__ refine,
-                                                       const uint32_t *__restrict__ listed)
+                                                       uint32_t *__restrict__ nine, const uint32_t *__restrict__ listed)
 {
     const uint64_t n = listed ? cc->nlisted : nprimes;
     if (cc->wide)
-        classify_range<FAM, Mont>(job, primes, n, codes, cc, refine, listed);
+        classify_range<FAM, Mont>(job, primes, n, codes, cc, refine, nine, listed);
     else
-        classify_range<FAM, MontN>(job, primes, n, codes, cc, refine, listed);
+        classify_range<FAM, MontN>(job, primes, n, codes, cc, refine, nine, listed);
 }
 
 template <uint32_t FAM, class MT>
 __device__ __forceinline__ void refine_range(const JobView &job, const uint64_t *__restrict__ primes,
                                              uint32_t *__restrict__ codes, ClassCounters *__restrict__ cc,
-                                             const uint32_t *__restrict__ refine, uint32_t n)
+                                             const uint32_t *__restrict__ refine, uint32_t *__restrict__ nine,
+                                             uint32_t n)
 {
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
         const uint32_t i = refine[t];
-        const uint32_t code = refined_code<FAM, MT>(job, primes[i], codes[i]);
+        const uint64_t p = primes[i];
+        const uint32_t code = refined_code<FAM, MT>(job, p, codes[i]);
         codes[i] = code;
-        if (code)
+        if (wants_nine(job, p, code))
+            nine[aggregated_increment(&cc->nnine, 0)] = i;
+        else if (code)
             aggregated_increment(cc->count, class_bucket(code >> 16));
     }
 }
@@ -1718,12 +1742,40 @@ __device__ __forceinline__ void refine_range(const JobView &job, const uint64_t 
 template <uint32_t FAM>
 __global__ void __launch_bounds__(256) refine_kernel(JobView job, const uint64_t *__restrict__ primes,
                                                      uint32_t *__restrict__ codes, ClassCounters *__restrict__ cc,
-                                                     const uint32_t *__restrict__ refine)
+                                                     const uint32_t *__restrict__ refine, uint32_t *__restrict__ nine)
 {
     if (cc->wide)
-        refine_range<FAM, Mont>(job, primes, codes, cc, refine, cc->nrefine);
+        refine_range<FAM, Mont>(job, primes, codes, cc, refine, nine, cc->nrefine);
     else
-        refine_range<FAM, MontN>(job, primes, codes, cc, refine, cc->nrefine);
+        refine_range<FAM, MontN>(job, primes, codes, cc, refine, nine, cc->nrefine);
+}
+
+template <uint32_t FAM, class MT>
+__device__ __forceinline__ void nine_range(const JobView &job, const uint64_t *__restrict__ primes,
+                                           uint32_t *__restrict__ codes, ClassCounters *__restrict__ cc,
+                                           const uint32_t *__restrict__ nine, uint32_t n)
+{
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+        const uint32_t i = nine[t];
+        const uint32_t code = nine_code<FAM, MT>(job, primes[i], codes[i]);
+        codes[i] = code;
+        if (code)
+            aggregated_increment(cc->count, class_bucket(code >> 16));
+    }
+}
+
+// The 9th-power character over the primes with 9 | p - 1 that classify or
+// the refinement listed (after the refinement, whose codes it narrows)
+template <uint32_t FAM>
+__global__ void __launch_bounds__(256) nine_kernel(JobView job, const uint64_t *__restrict__ primes,
+                                                   uint32_t *__restrict__ codes, ClassCounters *__restrict__ cc,
+                                                   const uint32_t *__restrict__ nine)
+{
+    if (cc->wide)
+        nine_range<FAM, Mont>(job, primes, codes, cc, nine, cc->nnine);
+    else
+        nine_range<FAM, MontN>(job, primes, codes, cc, nine, cc->nnine);
 }
 
 // Each CTA regroups tiles of 256 x REGROUP_PER_THREAD primes: a histogram of
@@ -2425,6 +2477,7 @@ void residue_scratch_destroy(ResidueScratch *rs)
     cudaFree(rs->items);
     cudaFree(rs->refine);
     cudaFree(rs->listed);
+    cudaFree(rs->nine);
     cudaFree(rs->counters);
     delete rs;
 }
@@ -2444,10 +2497,12 @@ static int ensure_class_scratch(ResidueScratch *rs, uint64_t nprimes, std::strin
     cudaFree(rs->items);
     cudaFree(rs->refine);
     cudaFree(rs->listed);
+    cudaFree(rs->nine);
     rs->codes = nullptr;
     rs->items = nullptr;
     rs->refine = nullptr;
     rs->listed = nullptr;
+    rs->nine = nullptr;
     rs->cap = 0;
     cudaError_t e = cudaMalloc(&rs->codes, nprimes * sizeof(uint32_t));
     if (e == cudaSuccess)
@@ -2456,6 +2511,8 @@ static int ensure_class_scratch(ResidueScratch *rs, uint64_t nprimes, std::strin
         e = cudaMalloc(&rs->refine, nprimes * sizeof(uint32_t));
     if (e == cudaSuccess)
         e = cudaMalloc(&rs->listed, nprimes * sizeof(uint32_t));
+    if (e == cudaSuccess)
+        e = cudaMalloc(&rs->nine, nprimes * sizeof(uint32_t));
     if (e != cudaSuccess) {
         err = std::string("class scratch: ") + cudaGetErrorString(e);
         return e == cudaErrorMemoryAllocation ? CTD_ERR_OUT_OF_MEMORY : CTD_ERR_CUDA;
@@ -2495,7 +2552,8 @@ static int launch_classified(const JobView &v, const uint64_t *d_primes, uint64_
             note_kernel_launch();
     }
     if (e == cudaSuccess) {
-        classify_kernel<FAM><<<cgrid, 256, 0, st>>>(v, d_primes, n, rs->codes, rs->counters, rs->refine, listed);
+        classify_kernel<FAM><<<cgrid, 256, 0, st>>>(v, d_primes, n, rs->codes, rs->counters, rs->refine, rs->nine,
+                                                    listed);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) {
@@ -2503,8 +2561,13 @@ static int launch_classified(const JobView &v, const uint64_t *d_primes, uint64_
         // the listed primes are about a quarter of n: a grid for that many
         const uint64_t rwant = (n / 4 + 255) / 256;
         const int rgrid = (int)(rwant < (uint64_t)rs->sm_count * 8 ? (rwant ? rwant : 1) : (uint64_t)rs->sm_count * 8);
-        refine_kernel<FAM><<<rgrid, 256, 0, st>>>(v, d_primes, rs->codes, rs->counters, rs->refine);
+        refine_kernel<FAM><<<rgrid, 256, 0, st>>>(v, d_primes, rs->codes, rs->counters, rs->refine, rs->nine);
         e = cudaGetLastError();
+        if (e == cudaSuccess) {
+            note_kernel_launch();
+            nine_kernel<FAM><<<rgrid, 256, 0, st>>>(v, d_primes, rs->codes, rs->counters, rs->nine);
+            e = cudaGetLastError();
+        }
     }
     if (e == cudaSuccess) {
         note_kernel_launch();
