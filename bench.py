@@ -416,10 +416,22 @@ def run_ours(args, world, rank, local):
             torch.distributed.all_reduce(tmax[:1], op=torch.distributed.ReduceOp.MAX)
             torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
             e2e_t, e2e_total = float(tmax[0]), float(t[1])
-        hbytes = sum(N * (4 + 8 * MAXF) for N in terms)
-        e2e = {"value": e2e_total / e2e_t, "unit": "updates/s", "h2d_bytes_per_step": hbytes,
-               "d2h_bytes_per_step": hbytes,
-               "api": "ctd_run_plain (include/ctd_gpu.h) per job with pinned host factors buffers, one segment per call"}
+        # bytes across the link per step, as ctd_run_plain moves them: a fresh
+        # (all-zero) resume state is cleared on the device, not uploaded; back
+        # come the counts and one record {term, count, slots} per term with hits
+        d2h = []
+        for j in range(steps):
+            b = 0
+            for buf in hsets[j]:
+                c = buf.counts.astype(np.int64)
+                b += 4 * len(c) + 8 + 8 * int((np.minimum(c, MAXF) + 2)[c > 0].sum())
+            d2h.append(b)
+        e2e = {"value": e2e_total / e2e_t, "unit": "updates/s", "h2d_bytes_per_step": 0,
+               "d2h_bytes_per_step": int(statistics.mean(d2h)),
+               "host_buffer_bytes_per_step": sum(N * (4 + 8 * MAXF) for N in terms),
+               "api": "ctd_run_plain (include/ctd_gpu.h) per job with pinned host factors buffers, one segment per "
+                      "call: the call reads the host resume state (all zeros: cleared on the device, nothing "
+                      "uploaded) and writes back the counts and the occupied slots"}
 
     if rank != 0:
         if world > 1:

@@ -35,6 +35,14 @@ struct ctd_ctx {
     size_t counts_cap = 0;
     uint64_t *d_factors = nullptr;
     size_t factors_cap = 0;
+    // the occupied slots of a factors buffer packed for the way back to the
+    // host (pack_occupied): device records, their length, pinned host copy
+    uint64_t *d_pack = nullptr;
+    size_t pack_cap = 0;
+    unsigned long long *d_pack_words = nullptr;
+    size_t pack_words_cap = 0;
+    uint64_t *h_pack = nullptr;
+    size_t h_pack_cap = 0;
     // per-family launch and tiling parameters (ctd_set_tuning / ctd_autotune)
     ctd_tuning tuning[10] = {};
     bool tuned[10] = {};
@@ -79,6 +87,100 @@ int ensure_buffer(ctd_ctx *ctx, T *&ptr, size_t &cap, size_t n)
     if (e != cudaSuccess)
         return cuda_fail(ctx, e, "cudaMalloc");
     cap = n;
+    return CTD_OK;
+}
+
+// ---- the factors buffer across the host link
+// A buffer holds max_factors slots a term and a few thousand hits a
+// segment: a call moves the counts and only the occupied slots.  A fresh
+// buffer (every count zero, so every slot zero) is cleared on the device
+// instead of copied; on the way back each term with hits becomes a record
+// {term, count, its min(count, max_factors) slots} in a packed device
+// buffer (record order is arrival order: the host places each by its term).
+__global__ void pack_occupied(const uint32_t *__restrict__ counts, const uint64_t *__restrict__ factors, uint64_t n,
+                              uint32_t maxf, uint64_t *__restrict__ pack, unsigned long long *__restrict__ words)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint32_t c = counts[i];
+        if (!c)
+            continue;
+        const uint32_t k = c < maxf ? c : maxf;
+        const unsigned long long at = atomicAdd(words, (unsigned long long)k + 2);
+        pack[at] = i;
+        pack[at + 1] = c;
+        for (uint32_t j = 0; j < k; ++j)
+            pack[at + 2 + j] = factors[i * maxf + j];
+    }
+}
+
+bool all_zero(const uint32_t *a, uint64_t n)
+{
+    for (uint64_t i = 0; i < n; ++i)
+        if (a[i])
+            return false;
+    return true;
+}
+
+// the resume state to the device: cleared there when it is all zeros
+int factors_to_device(ctd_ctx *ctx, const uint32_t *counts, const uint64_t *factors, uint64_t n, uint32_t maxf,
+                      cudaStream_t st)
+{
+    if (all_zero(counts, n)) {
+        CTX_CUDA(cudaMemsetAsync(ctx->d_counts, 0, n * sizeof(uint32_t), st));
+        CTX_CUDA(cudaMemsetAsync(ctx->d_factors, 0, n * maxf * sizeof(uint64_t), st));
+        return CTD_OK;
+    }
+    CTX_CUDA(cudaMemcpyAsync(ctx->d_counts, counts, n * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    CTX_CUDA(cudaMemcpyAsync(ctx->d_factors, factors, n * maxf * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+    return CTD_OK;
+}
+
+// the result to the host: the counts, then the occupied slots as records
+// (the whole factors array when the records would not be much smaller);
+// the host slots past a term's count keep their zeros
+int factors_to_host(ctd_ctx *ctx, uint32_t *counts, uint64_t *factors, uint64_t n, uint32_t maxf, cudaStream_t st)
+{
+    const uint64_t nf = n * maxf;
+    int rc = ensure_buffer(ctx, ctx->d_pack, ctx->pack_cap, nf + 2 * n);
+    if (!rc)
+        rc = ensure_buffer(ctx, ctx->d_pack_words, ctx->pack_words_cap, 1);
+    if (rc)
+        return rc;
+    CTX_CUDA(cudaMemcpyAsync(counts, ctx->d_counts, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CTX_CUDA(cudaMemsetAsync(ctx->d_pack_words, 0, sizeof(unsigned long long), st));
+    const uint64_t want = (n + 255) / 256;
+    const int grid = (int)(want < (uint64_t)ctx->sm_count * 4 ? (want ? want : 1) : (uint64_t)ctx->sm_count * 4);
+    pack_occupied<<<grid, 256, 0, st>>>(ctx->d_counts, ctx->d_factors, n, maxf, ctx->d_pack, ctx->d_pack_words);
+    CTX_CUDA(cudaGetLastError());
+    note_kernel_launch();
+    unsigned long long words = 0;
+    CTX_CUDA(cudaMemcpyAsync(&words, ctx->d_pack_words, sizeof(words), cudaMemcpyDeviceToHost, st));
+    CTX_CUDA(cudaStreamSynchronize(st));
+    if (words * 2 > nf) {
+        CTX_CUDA(cudaMemcpyAsync(factors, ctx->d_factors, nf * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+        CTX_CUDA(cudaStreamSynchronize(st));
+        return CTD_OK;
+    }
+    if (words > ctx->h_pack_cap) {
+        cudaFreeHost(ctx->h_pack);
+        ctx->h_pack = nullptr;
+        ctx->h_pack_cap = 0;
+        const size_t cap = words < 4096 ? 4096 : 2 * words;
+        CTX_CUDA(cudaMallocHost(&ctx->h_pack, cap * sizeof(uint64_t)));
+        ctx->h_pack_cap = cap;
+    }
+    if (words) {
+        CTX_CUDA(cudaMemcpyAsync(ctx->h_pack, ctx->d_pack, words * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+        CTX_CUDA(cudaStreamSynchronize(st));
+    }
+    for (uint64_t at = 0; at < words;) {
+        const uint64_t i = ctx->h_pack[at];
+        const uint64_t c = ctx->h_pack[at + 1];
+        const uint64_t k = c < maxf ? c : maxf;
+        std::memcpy(factors + i * maxf, ctx->h_pack + at + 2, k * sizeof(uint64_t));
+        at += k + 2;
+    }
     return CTD_OK;
 }
 
@@ -333,6 +435,9 @@ void ctd_close(ctd_ctx *ctx)
     cudaFree(ctx->d_primes);
     cudaFree(ctx->d_counts);
     cudaFree(ctx->d_factors);
+    cudaFree(ctx->d_pack);
+    cudaFree(ctx->d_pack_words);
+    cudaFreeHost(ctx->h_pack);
     if (ctx->stream)
         cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -728,8 +833,9 @@ int ctd_run_plain(ctd_ctx *ctx, const ctd_job *job, uint32_t *counts_inout, uint
         return rc;
     cudaStream_t st = ctx->stream;
     // the resume state (zeros for a fresh job) goes to the device once
-    CTX_CUDA(cudaMemcpyAsync(ctx->d_counts, counts_inout, N * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-    CTX_CUDA(cudaMemcpyAsync(ctx->d_factors, factors_inout, NF * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+    rc = factors_to_device(ctx, counts_inout, factors_inout, N, job->max_factors, st);
+    if (rc)
+        return rc;
     JobView view = make_view(job, ctx->d_counts, ctx->d_factors);
     std::string err;
 
@@ -798,10 +904,7 @@ int ctd_run_plain(ctd_ctx *ctx, const ctd_job *job, uint32_t *counts_inout, uint
         if (fy == f1)
             break;
     }
-    CTX_CUDA(cudaMemcpyAsync(counts_inout, ctx->d_counts, N * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    CTX_CUDA(cudaMemcpyAsync(factors_inout, ctx->d_factors, NF * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
-    CTX_CUDA(cudaStreamSynchronize(st));
-    return CTD_OK;
+    return factors_to_host(ctx, counts_inout, factors_inout, N, job->max_factors, st);
 }
 
 }  // extern "C"

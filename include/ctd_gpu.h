@@ -174,7 +174,11 @@ int ctd_check_job(const ctd_job *job);
  * max_factors smallest and its count exceeds max_factors: the CPU engine's
  * result; the reference's device push keeps whichever arrive first and both
  * report the excess (src/factors_buffer.hpp:62-75).  Primes p <= resume_after_prime are
- * skipped (src/trial_factoring.cuh:404).  segment_length 0 = default 2^26.
+ * skipped (src/trial_factoring.cuh:404).  segment_length 0 = the tuned
+ * length for the job's family and first prime width (2^26 untuned).  Across
+ * the host link the call moves only what it must: an all-zero resume state
+ * is cleared on the device instead of uploaded, and the counts come back
+ * with the occupied slots only (the host slots past a count stay zero).
  */
 int ctd_run_plain(ctd_ctx *ctx, const ctd_job *job, uint32_t *counts_inout, uint64_t *factors_inout,
                   uint64_t resume_after_prime, uint64_t segment_length, ctd_progress_cb cb, void *user);
