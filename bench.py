@@ -82,9 +82,9 @@ FAMILY_NAMES = {0: "MERSENNE", 1: "PROTH", 2: "RIESEL", 3: "SMARANDACHE", 4: "FI
                 6: "PROTH_FIXED_N", 7: "RIESEL_FIXED_N", 8: "TRIBONACCI"}
 # Roofline inputs per workload (what the dominant launch executes):
 #  * proth -- the classified doubling launch (screen_kernel, classify_kernel,
-#    refine_kernel, regroup_kernel, class_walk_kernel): bound by integer
-#    issue slots.  Thread instructions and DRAM bytes per prime come from one
-#    ncu capture of the same five kernels on the 2^27-wide segment
+#    refine_kernel, nine_kernel, regroup_kernel, class_walk_kernel): bound by
+#    integer issue slots.  Thread instructions and DRAM bytes per prime come
+#    from one ncu capture of the same six kernels on the 2^27-wide segment
 #    [2^32, 2^32 + 2^27) of this workload
 #    (6,047,768 primes; the capture's command is in the profile summary);
 #    the live launch time comes from CUDA events in this run.
@@ -96,11 +96,11 @@ FAMILY_NAMES = {0: "MERSENNE", 1: "PROTH", 2: "RIESEL", 3: "SMARANDACHE", 4: "FI
 #    shifts per block = 57/18 ALU operations per update, against the ALU
 #    compare rate measured now.
 PROTH_NCU = {"primes": 6047768,
-             "thread_inst": {"screen_kernel": 56524200 * 30.87, "classify_kernel": 1193287874 * 25.31,
-                             "refine_kernel": 301277230 * 24.99, "regroup_kernel": 53971012 * 16.98,
-                             "class_walk_kernel": 2108416057 * 29.62},
-             "dram_bytes": (59.566336 + 12.364544 + 76.983808 + 13.673984 + 78.414592 + 1.666560 + 72.933632
-                            + 12.878336 + 54.180864 + 7.825920) * 1e6}
+             "thread_inst": {"screen_kernel": 56524200 * 30.87, "classify_kernel": 1138696783 * 24.99,
+                             "refine_kernel": 288371018 * 24.44, "nine_kernel": 89598023 * 28.62,
+                             "regroup_kernel": 54846300 * 16.45, "class_walk_kernel": 1943662882 * 29.43},
+             "dram_bytes": (59.647488 + 12.317696 + 77.039616 + 13.650176 + 78.412288 + 1.800960 + 68.404480
+                            + 1.362176 + 72.984832 + 13.078528 + 53.844736 + 7.384576) * 1e6}
 SMARANDACHE_MULS_PER_UPDATE = 3
 TRIBONACCI_ALU_OPS_PER_UPDATE = 57 / 18
 
@@ -450,12 +450,12 @@ def run_ours(args, world, rank, local):
         achieved = inst / launch_s
         roofline = {
             "bound": "int_issue",
-            "kernel": "screen_kernel<PROTH> + classify_kernel<PROTH> + refine_kernel<PROTH> + regroup_kernel + "
-                      "class_walk_kernel<PROTH>",
+            "kernel": "screen_kernel<PROTH> + classify_kernel<PROTH> + refine_kernel<PROTH> + nine_kernel<PROTH> + "
+                      "regroup_kernel + class_walk_kernel<PROTH>",
             "achieved": achieved / 1e9, "peak": (peaks["int"] / 1e9) if peaks["int"] else None, "unit": "Ginst/s",
             "frac": (achieved / peaks["int"]) if peaks["int"] else None,
             "thread_instructions_per_update": inst / per_launch_updates, "launch_ms": launch_s * 1e3,
-            "achieved_source": "ncu thread instructions of the five kernels on a 2^27-segment of this workload, "
+            "achieved_source": "ncu thread instructions of the six kernels on a 2^27-segment of this workload, "
                                "scaled by the primes per launch, over the CUDA-event launch time of this run",
             "peak_source": "measured now: libctd_probe add/xor chains (integer issue rate) on this GPU",
             "traffic": PROTH_NCU["dram_bytes"] / PROTH_NCU["primes"] * primes_launch,
