@@ -225,6 +225,57 @@ using Mont = MontT<false>;
 using MontN = MontT<true>;  // p < 2^40
 constexpr uint64_t MONT_NARROW_LIMIT = 1ull << 40;
 
+// ------------------------------------------------------- Montgomery, R=2^32
+// The same interface for an odd p < 2^31 (values in uint64, below p): a
+// product is one 32x32 multiply, m = T pinv mod 2^32 and one multiply-add,
+// (T + m p) / 2^32 < 2p -- a few instructions where the R = 2^64 form takes
+// about forty.  For the per-prime set-up of walks whose primes fit 31 bits.
+struct Mont32 {
+    uint64_t p;
+    uint64_t pinv;  // -p^-1 mod 2^32
+    uint64_t one;   // 2^32 mod p
+    uint64_t r2;    // 2^64 mod p
+
+    CTD_HD void init(uint64_t modulus)
+    {
+        p = modulus;
+        const uint32_t p32 = (uint32_t)p;
+        uint32_t x = p32;  // p^-1 mod 2^32 by Newton-Hensel lifting
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            x *= 2u - p32 * x;
+        pinv = (uint32_t)(0u - x);
+        one = (uint64_t)(0xffffffffu % p32 + 1u) % p32;
+        r2 = one * one % p;
+    }
+    CTD_HD uint64_t mul(uint64_t a, uint64_t b) const
+    {
+        const uint64_t T = a * b;  // < 2^62
+        const uint32_t m = (uint32_t)T * (uint32_t)pinv;
+        const uint64_t r = (T + (uint64_t)m * p) >> 32;
+        return r >= p ? r - p : r;
+    }
+    CTD_HD uint64_t to(uint64_t x) const { return mul(x < p ? x : x % p, r2); }
+    CTD_HD uint64_t from(uint64_t X) const { return mul(X, 1); }
+    CTD_HD uint64_t add(uint64_t a, uint64_t b) const { return addmod(a, b, p); }
+    CTD_HD uint64_t sub(uint64_t a, uint64_t b) const { return submod(a, b, p); }
+    CTD_HD uint64_t dbl(uint64_t a) const { return dblmod(a, p); }
+    CTD_HD uint64_t pow(uint64_t base, uint64_t e) const
+    {
+        uint64_t r = one;
+        while (e) {
+            if (e & 1)
+                r = mul(r, base);
+            base = mul(base, base);
+            e >>= 1;
+        }
+        return r;
+    }
+    // Shoup's quotient floor(w 2^32 / p) of the plain w whose Montgomery form
+    // is W: w 2^32 = q p + W, so q = -W p^-1 = W pinv mod 2^32 (exact: q < 2^32)
+    CTD_HD uint32_t shoup_of_form(uint64_t W) const { return (uint32_t)W * (uint32_t)pinv; }
+};
+
 // ------------------------------------------------------ Shoup, 32-bit words
 // x * w mod p with the precomputed quotient ws = floor(w * 2^32 / p)
 // (Shoup, "NTL: A library for doing number theory"; also Harvey 2014).

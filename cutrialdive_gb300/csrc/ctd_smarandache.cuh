@@ -51,7 +51,8 @@ CTD_HD uint32_t digit_count(uint64_t b, uint64_t m)
 
 // the multiplier b^len(m) mod p (plain) of the digit class holding m, given
 // class_end's pw for m
-CTD_HD uint64_t class_multiplier(const Mont &m, uint64_t b, uint64_t mcur, uint64_t pw)
+template <class MT>
+CTD_HD uint64_t class_multiplier(const MT &m, uint64_t b, uint64_t mcur, uint64_t pw)
 {
     if (pw != ~0ull)
         return pw < m.p ? pw : pw % m.p;
@@ -62,7 +63,8 @@ CTD_HD uint64_t class_multiplier(const Mont &m, uint64_t b, uint64_t mcur, uint6
 // (Montgomery form).  Left-to-right over the bits of t, keeping (M^k, G(k),
 // H(k), k) for the prefix k read so far; k itself is kept in Montgomery form
 // (K) and updated by doubling and adding one, so no conversion is needed.
-CTD_HD uint64_t affine_jump(const Mont &m, uint64_t X, uint64_t Mm, uint64_t c0, uint64_t t)
+template <class MT>
+CTD_HD uint64_t affine_jump(const MT &m, uint64_t X, uint64_t Mm, uint64_t c0, uint64_t t)
 {
     if (!t)
         return X;
@@ -89,7 +91,8 @@ CTD_HD uint64_t affine_jump(const Mont &m, uint64_t X, uint64_t Mm, uint64_t c0,
 
 // Sm_b(s) mod p in Montgomery form by class-by-class doubling jumps (needs
 // m.r2).
-CTD_HD uint64_t smarandache_at_doubling(const Mont &m, uint64_t b, uint64_t s)
+template <class MT>
+CTD_HD uint64_t smarandache_at_doubling(const MT &m, uint64_t b, uint64_t s)
 {
     uint64_t X = 0;
     uint64_t c = 1;  // next m to apply
@@ -109,7 +112,8 @@ constexpr int SM_MAX_CLASSES = 24;
 
 // Sm_b(s) mod p in Montgomery form by the closed-form class jumps (needs
 // m.r2; p prime, for the Fermat inversion).
-CTD_HD uint64_t smarandache_at_closed(const Mont &m, uint64_t b, uint64_t s)
+template <class MT>
+CTD_HD uint64_t smarandache_at_closed(const MT &m, uint64_t b, uint64_t s)
 {
     // the digit classes of 1 .. s: [lo_d, hi_d], multiplier Md (Montgomery form)
     uint64_t Mt[SM_MAX_CLASSES];   // M_d
@@ -165,7 +169,8 @@ CTD_HD uint64_t smarandache_at_closed(const Mont &m, uint64_t b, uint64_t s)
 // per bit of each class length; the closed form about 1.5 per bit (the powers
 // M^t), 8 per class and 1.5 per bit of p (the one inversion), so short
 // prefixes -- a few classes of a few terms -- go by doubling.
-CTD_HD uint64_t smarandache_at(const Mont &m, uint64_t b, uint64_t s)
+template <class MT>
+CTD_HD uint64_t smarandache_at(const MT &m, uint64_t b, uint64_t s)
 {
     uint32_t bits = 0, classes = 0;
     for (uint64_t c = 1; c <= s;) {
