@@ -1410,7 +1410,8 @@ __device__ __forceinline__ void run_smarandache(const JobView &job, uint64_t p, 
         // so x = 0 mod p <=> x == p or x == 2p (x >= 1 after a step).  The
         // set-up (the jump to Sm_b(s), the class multipliers and their Shoup
         // quotients) in 32-bit Montgomery arithmetic: with the 64-bit form it
-        // was about 40 % of configuration 1's instructions (991 steps a prime)
+        // was about 40 % of the instructions of base 10 over n = 10..1000
+        // (991 steps a prime) with every prime below 2^28
         Mont32 m;
         m.init(p);
         const uint64_t X = smarandache_at(m, b, s);
