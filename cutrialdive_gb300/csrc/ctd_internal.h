@@ -114,7 +114,7 @@ struct ClassCounters {
     uint32_t fill[CLASS_BUCKETS];   // regroup cursors
     unsigned long long next;        // walk work counter
     uint32_t nrefine;               // primes listed for the rare-prime refinement
-    uint32_t nlisted;               // primes the quadratic screen left for classification
+    uint32_t nlisted[8];            // primes the screen left for classification, by divisibility pattern
     uint32_t wide;                  // a prime of the launch is 2^40 or above
     uint32_t nnine;                 // primes listed for the 9th-power character
 };
@@ -130,7 +130,7 @@ struct ResidueScratch {
     uint32_t *codes = nullptr;
     ClassItem *items = nullptr;
     uint32_t *refine = nullptr;  // indices of the primes to refine
-    uint32_t *listed = nullptr;  // indices of the primes to classify
+    uint32_t *listed = nullptr;  // indices of the primes to classify: 8 lists of cap, by pattern
     uint32_t *nine = nullptr;    // indices of the primes for the 9th-power character
     uint64_t cap = 0;  // primes
     ClassCounters *counters = nullptr;

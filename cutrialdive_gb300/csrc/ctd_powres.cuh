@@ -331,6 +331,168 @@ CTD_HD PowerClass doubling_class(const MT &m, uint64_t k, bool negate)
     return c;
 }
 
+// ---- the same class for a known divisibility pattern of p - 1
+// PAT bit 0: 3 | p - 1, bit 1: 5 | p - 1, bit 2: 7 | p - 1.  A q that does
+// not divide p - 1 gives no condition (x -> x^q permutes the group), so the
+// kernels, which bucket the primes by pattern first, raise A and B only to
+// the exponents the pattern needs: on average about 2.5 products for the
+// odd part instead of the 11 of the full chain, one q's squarings and scan
+// instead of three.  Every lane of a bucket runs the same code.
+CTD_HD uint32_t powres_pattern(uint64_t p)
+{
+    return ((p - 1) % 3 == 0 ? 1u : 0u) | ((p - 1) % 5 == 0 ? 2u : 0u) | ((p - 1) % 7 == 0 ? 4u : 0u);
+}
+
+// x^D and x^(D/q) for the q of PAT, D the product of PAT's q: short chains
+template <int PAT, class MT>
+CTD_HD void odd_powers(const MT &m, uint64_t x, uint64_t &xd, uint64_t (&xq)[3])
+{
+    auto mul = [&](uint64_t a, uint64_t b) { return powres_mul<MT>(a, b, m.p, m.pinv); };
+    xq[0] = xq[1] = xq[2] = x;
+    if constexpr (PAT == 0) {
+        xd = x;
+    } else if constexpr (PAT == 1) {  // 3
+        xd = mul(mul(x, x), x);
+    } else if constexpr (PAT == 2) {  // 5
+        const uint64_t x2 = mul(x, x), x4 = mul(x2, x2);
+        xd = mul(x4, x);
+    } else if constexpr (PAT == 4) {  // 7
+        const uint64_t x3 = mul(mul(x, x), x), x6 = mul(x3, x3);
+        xd = mul(x6, x);
+    } else if constexpr (PAT == 3) {  // 15 = 3 5
+        const uint64_t x2 = mul(x, x), x3 = mul(x2, x), x5 = mul(x3, x2), x10 = mul(x5, x5);
+        xd = mul(x10, x5);
+        xq[0] = x5;
+        xq[1] = x3;
+    } else if constexpr (PAT == 5) {  // 21 = 3 7
+        const uint64_t x2 = mul(x, x), x3 = mul(x2, x), x4 = mul(x2, x2), x7 = mul(x4, x3), x14 = mul(x7, x7);
+        xd = mul(x14, x7);
+        xq[0] = x7;
+        xq[2] = x3;
+    } else if constexpr (PAT == 6) {  // 35 = 5 7
+        const uint64_t x2 = mul(x, x), x3 = mul(x2, x), x5 = mul(x3, x2), x7 = mul(x5, x2);
+        const uint64_t x14 = mul(x7, x7), x28 = mul(x14, x14);
+        xd = mul(x28, x7);
+        xq[1] = x7;
+        xq[2] = x5;
+    } else {  // 105
+        const Pow105 c = pow105(m, x);
+        xd = c.p105;
+        xq[0] = c.p35;
+        xq[1] = c.p21;
+        xq[2] = c.p15;
+    }
+}
+
+// doubling_class for a p whose pattern is PAT (powres_pattern(p) == PAT)
+template <int PAT, class MT>
+CTD_HD PowerClass doubling_class_pat(const MT &m, uint64_t k, bool negate)
+{
+    const uint64_t p = m.p;
+    const uint64_t p1 = p - 1;
+#ifdef __CUDA_ARCH__
+    const int v = __ffsll((long long)p1) - 1;
+#else
+    const int v = __builtin_ctzll(p1);
+#endif
+    const int u = v < POWRES_MAX_2EXP ? v : POWRES_MAX_2EXP;
+    // e0 = (p - 1) / D, D = 2^u 3^f3 5^f5 7^f7 (divisions by constants)
+    uint64_t e0 = p1 >> u;
+    if constexpr ((PAT & 1) != 0)
+        e0 /= 3;
+    if constexpr ((PAT & 2) != 0)
+        e0 /= 5;
+    if constexpr ((PAT & 4) != 0)
+        e0 /= 7;
+    auto mul = [&](uint64_t a, uint64_t b) { return powres_mul<MT>(a, b, p, m.pinv); };
+    uint64_t A, B;
+    power_pair(m, k, negate, e0, A, B);
+    uint64_t ad, bd, aq[3], bq[3];
+    odd_powers<PAT>(m, A, ad, aq);
+    odd_powers<PAT>(m, B, bd, bq);
+    PowerClass c{1, 0};
+    // ---- the 2-power part: z = A^D_odd of order 2^i (i <= u)
+    {
+        const uint64_t z = ad, y = bd;
+        uint64_t zs = z, ys = y;
+        int i = 0;
+        bool y_ok = ys == m.one;
+        bool found = zs == m.one;
+#pragma unroll
+        for (int t = 1; t <= POWRES_MAX_2EXP; ++t) {
+            zs = mul(zs, zs);
+            ys = mul(ys, ys);
+            if (!found && t <= u) {
+                i = t;
+                y_ok = ys == m.one;
+                found = zs == m.one;
+            }
+        }
+        if (!y_ok)
+            return PowerClass{0, 0};
+        uint32_t j = 0;
+        uint64_t t = m.one;
+#pragma unroll
+        for (uint32_t jj = 0; jj < (1u << POWRES_MAX_2EXP); ++jj) {
+            if (jj < (1u << i) && t == y)
+                j = jj;
+            if (jj + 1 < (1u << POWRES_MAX_2EXP))
+                t = mul(t, z);
+        }
+        c.M = 1u << i;
+        c.r = j;
+    }
+    // ---- the q of PAT: z = (A^(D_odd/q))^(2^u)
+    const uint32_t qs[3] = {3, 5, 7};
+#pragma unroll
+    for (int kq = 0; kq < 3; ++kq) {
+        if (!((PAT >> kq) & 1))
+            continue;
+        const uint32_t q = qs[kq];
+        uint64_t z = aq[kq], y = bq[kq];
+#pragma unroll
+        for (int t = 0; t < POWRES_MAX_2EXP; ++t) {
+            const uint64_t z2 = mul(z, z), y2 = mul(y, y);
+            z = t < u ? z2 : z;
+            y = t < u ? y2 : y;
+        }
+        if (z == m.one) {
+            if (y != m.one)
+                return PowerClass{0, 0};
+            continue;
+        }
+        uint32_t j = q;
+        uint64_t t = m.one;
+#pragma unroll
+        for (uint32_t jj = 0; jj < q; ++jj) {
+            if (t == y)
+                j = jj;
+            if (jj + 1 < q)
+                t = mul(t, z);
+        }
+        if (j >= q)  // cannot happen for prime p
+            return PowerClass{1, 0};
+        crt_merge_small(c, j, q);
+    }
+    return c;
+}
+
+// doubling_class_pat for p's own pattern (host checks)
+template <class MT>
+inline PowerClass doubling_class_by_pattern(const MT &m, uint64_t k, bool negate)
+{
+    switch (powres_pattern(m.p)) {
+    case 0: return doubling_class_pat<0>(m, k, negate);
+    case 1: return doubling_class_pat<1>(m, k, negate);
+    case 2: return doubling_class_pat<2>(m, k, negate);
+    case 3: return doubling_class_pat<3>(m, k, negate);
+    case 4: return doubling_class_pat<4>(m, k, negate);
+    case 5: return doubling_class_pat<5>(m, k, negate);
+    case 6: return doubling_class_pat<6>(m, k, negate);
+    default: return doubling_class_pat<7>(m, k, negate);
+    }
+}
+
 // ---- refinement by the character of a rarer prime q = 11 .. 61
 // A prime q divides p - 1 for one prime p in q - 1, and then its character
 // keeps one term in q (or none), so over the classes above the walk shrinks

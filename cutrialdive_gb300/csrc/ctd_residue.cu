@@ -1671,26 +1671,71 @@ __device__ __forceinline__ uint32_t refined_code(const JobView &job, uint64_t p,
 // its warps spend the two powers on primes that need them.  Every family:
 // cc->wide is set when a prime is 2^40 or above (the class kernels then take
 // the general Montgomery product instead of the narrow one).
+// Tiles of 256 x SCREEN_PER_THREAD primes per CTA: the listed primes are
+// counted per pattern in shared memory and each tile takes its places in
+// the eight lists with one global atomic per pattern (a global atomic per
+// pattern and warp doubled the kernel's time).
+constexpr int SCREEN_PER_THREAD = 8;
 template <uint32_t FAM>
 __global__ void __launch_bounds__(256) screen_kernel(JobView job, const uint64_t *__restrict__ primes,
                                                      uint64_t nprimes, uint32_t *__restrict__ codes,
-                                                     ClassCounters *__restrict__ cc, uint32_t *__restrict__ listed)
+                                                     ClassCounters *__restrict__ cc, uint32_t *__restrict__ listed,
+                                                     uint64_t cap)
 {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nprimes; i += stride) {
-        const uint64_t p = primes[i];
-        if (p >= MONT_NARROW_LIMIT)
-            cc->wide = 1;
-        if (!listed)
-            continue;
-        if (quadratic_excluded(p, job.param, FAM == PROTH))
-            codes[i] = 0;
-        else
-            listed[aggregated_increment(&cc->nlisted, 0)] = (uint32_t)i;
+    __shared__ uint32_t hist[8], tile_base[8];
+    const uint32_t tid = threadIdx.x;
+    const uint64_t tile = (uint64_t)blockDim.x * SCREEN_PER_THREAD;
+    bool wide = false;
+    for (uint64_t t0 = (uint64_t)blockIdx.x * tile; t0 < nprimes; t0 += (uint64_t)gridDim.x * tile) {
+        if (tid < 8)
+            hist[tid] = 0;
+        __syncthreads();
+        uint32_t pat[SCREEN_PER_THREAD], off[SCREEN_PER_THREAD];
+#pragma unroll
+        for (int j = 0; j < SCREEN_PER_THREAD; ++j) {
+            const uint64_t i = t0 + (uint64_t)j * blockDim.x + tid;
+            pat[j] = 8;  // nothing to list
+            if (i < nprimes) {
+                const uint64_t p = primes[i];
+                wide |= p >= MONT_NARROW_LIMIT;
+                if (FAM != MERSENNE && quadratic_excluded(p, job.param, FAM == PROTH))
+                    codes[i] = 0;
+                else
+                    pat[j] = powres_pattern(p);
+            }
+            if (pat[j] < 8)
+                off[j] = aggregated_increment(hist, pat[j]);
+        }
+        __syncthreads();
+        if (tid < 8)
+            tile_base[tid] = hist[tid] ? atomicAdd(&cc->nlisted[tid], hist[tid]) : 0u;
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < SCREEN_PER_THREAD; ++j)
+            if (pat[j] < 8)
+                listed[pat[j] * cap + tile_base[pat[j]] + off[j]] = (uint32_t)(t0 + (uint64_t)j * blockDim.x + tid);
+        __syncthreads();
     }
+    if (wide)
+        cc->wide = 1;
 }
 
-template <uint32_t FAM, class MT>
+// the class code of a prime whose divisibility pattern is PAT
+template <uint32_t FAM, int PAT, class MT>
+__device__ __forceinline__ uint32_t class_code_pat(const JobView &job, uint64_t p)
+{
+    if (p >= (1ull << 63))
+        return 1u << 16;
+    const uint64_t k = FAM == MERSENNE ? 1 : (job.param < p ? job.param : job.param % p);
+    if (!k)
+        return 0;
+    MT m;
+    m.init(p);
+    const PowerClass c = doubling_class_pat<PAT>(m, k, FAM == PROTH);
+    return c.M ? (c.M << 16) | c.r : 0u;
+}
+
+template <uint32_t FAM, int PAT, class MT>
 __device__ __forceinline__ void classify_range(const JobView &job, const uint64_t *__restrict__ primes, uint64_t n,
                                                uint32_t *__restrict__ codes, ClassCounters *__restrict__ cc,
                                                uint32_t *__restrict__ refine, uint32_t *__restrict__ nine,
@@ -1698,9 +1743,9 @@ __device__ __forceinline__ void classify_range(const JobView &job, const uint64_
 {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
-        const uint64_t i = listed ? listed[t] : t;
+        const uint64_t i = listed[t];
         const uint64_t p = primes[i];
-        const uint32_t code = doubling_class_code<FAM, MT>(job, p);
+        const uint32_t code = class_code_pat<FAM, PAT, MT>(job, p);
         codes[i] = code;
         if (wants_refine(job, p, code))
             refine[aggregated_increment(&cc->nrefine, 0)] = (uint32_t)i;
@@ -1711,19 +1756,21 @@ __device__ __forceinline__ void classify_range(const JobView &job, const uint64_
     }
 }
 
-// the classes of the listed primes (all primes when `listed` is null), by
-// the narrow Montgomery product unless the screen saw a prime of 2^40 or more
-template <uint32_t FAM>
+// the classes of the primes the screen listed under divisibility pattern
+// PAT, by the narrow Montgomery product unless the screen saw a prime of
+// 2^40 or more (one launch per pattern: every lane of a launch runs the
+// same chains)
+template <uint32_t FAM, int PAT>
 __global__ void __launch_bounds__(256, 4) classify_kernel(JobView job, const uint64_t *__restrict__ primes,
-                                                       uint64_t nprimes, uint32_t *__restrict__ codes,
-                                                       ClassCounters *__restrict__ cc, uint32_t *__restrict__ refine,
-                                                       uint32_t *__restrict__ nine, const uint32_t *__restrict__ listed)
+                                                       uint32_t *__restrict__ codes, ClassCounters *__restrict__ cc,
+                                                       uint32_t *__restrict__ refine, uint32_t *__restrict__ nine,
+                                                       const uint32_t *__restrict__ listed, uint64_t cap)
 {
-    const uint64_t n = listed ? cc->nlisted : nprimes;
+    const uint64_t n = cc->nlisted[PAT];
     if (cc->wide)
-        classify_range<FAM, Mont>(job, primes, n, codes, cc, refine, nine, listed);
+        classify_range<FAM, PAT, Mont>(job, primes, n, codes, cc, refine, nine, listed + PAT * cap);
     else
-        classify_range<FAM, MontN>(job, primes, n, codes, cc, refine, nine, listed);
+        classify_range<FAM, PAT, MontN>(job, primes, n, codes, cc, refine, nine, listed + PAT * cap);
 }
 
 template <uint32_t FAM, class MT>
@@ -2518,7 +2565,7 @@ static int ensure_class_scratch(ResidueScratch *rs, uint64_t nprimes, std::strin
     if (e == cudaSuccess)
         e = cudaMalloc(&rs->refine, nprimes * sizeof(uint32_t));
     if (e == cudaSuccess)
-        e = cudaMalloc(&rs->listed, nprimes * sizeof(uint32_t));
+        e = cudaMalloc(&rs->listed, 8 * nprimes * sizeof(uint32_t));
     if (e == cudaSuccess)
         e = cudaMalloc(&rs->nine, nprimes * sizeof(uint32_t));
     if (e != cudaSuccess) {
@@ -2550,20 +2597,26 @@ static int launch_classified(const JobView &v, const uint64_t *d_primes, uint64_
     cudaError_t e = cudaMemsetAsync(rs->counters, 0, sizeof(ClassCounters), st);
     const uint64_t want = (n + 255) / 256;
     const int cgrid = (int)(want < (uint64_t)rs->sm_count * 8 ? want : (uint64_t)rs->sm_count * 8);
-    // the quadratic screen (Mersenne's target 1 is always a residue: its
-    // pass only looks for primes of 2^40 and above)
-    uint32_t *listed = FAM == MERSENNE ? nullptr : rs->listed;
+    // the quadratic screen (Mersenne's target 1 is always a residue) and the
+    // primes' buckets by divisibility pattern, then one classification
+    // launch per pattern
     if (e == cudaSuccess) {
-        screen_kernel<FAM><<<cgrid, 256, 0, st>>>(v, d_primes, n, rs->codes, rs->counters, listed);
+        screen_kernel<FAM><<<cgrid, 256, 0, st>>>(v, d_primes, n, rs->codes, rs->counters, rs->listed, rs->cap);
         e = cudaGetLastError();
         if (e == cudaSuccess)
             note_kernel_launch();
     }
-    if (e == cudaSuccess) {
-        classify_kernel<FAM><<<cgrid, 256, 0, st>>>(v, d_primes, n, rs->codes, rs->counters, rs->refine, rs->nine,
-                                                    listed);
-        e = cudaGetLastError();
+#define CTD_CLASSIFY(PAT)                                                                                         \
+    if (e == cudaSuccess) {                                                                                       \
+        classify_kernel<FAM, PAT><<<cgrid, 256, 0, st>>>(v, d_primes, rs->codes, rs->counters, rs->refine,       \
+                                                         rs->nine, rs->listed, rs->cap);                          \
+        e = cudaGetLastError();                                                                                   \
+        if (e == cudaSuccess && PAT < 7)                                                                          \
+            note_kernel_launch();                                                                                 \
     }
+    CTD_CLASSIFY(0) CTD_CLASSIFY(1) CTD_CLASSIFY(2) CTD_CLASSIFY(3)
+    CTD_CLASSIFY(4) CTD_CLASSIFY(5) CTD_CLASSIFY(6) CTD_CLASSIFY(7)
+#undef CTD_CLASSIFY
     if (e == cudaSuccess) {
         note_kernel_launch();
         // the listed primes are about a quarter of n: a grid for that many

@@ -6,7 +6,8 @@
 // the 9th-power character when 9 | p - 1; M = 0 (M2 = 0)
 // when no n does; then "x" (1 when the quadratic screen excludes p) and the
 // Jacobi symbol (wt/p); last 1 when the classes through the narrow
-// Montgomery product (p < 2^40) equal these (always 1 above 2^40).
+// Montgomery product (p < 2^40) and the class for p's divisibility pattern
+// (doubling_class_pat) equal these.
 #include <cinttypes>
 #include <cstdio>
 
@@ -24,7 +25,8 @@ int main()
         if ((p - 1) % 9 == 0)
             f = ctd::nine_class(m, p - wt, true, f);
         const int x = ctd::quadratic_excluded(p, p - wt, true) ? 1 : 0;
-        int same = 1;
+        const ctd::PowerClass cp = ctd::doubling_class_by_pattern(m, p - wt, true);
+        int same = cp.M == c.M && cp.r == c.r;
         if (p < ctd::MONT_NARROW_LIMIT) {
             ctd::MontN n;
             n.init(p);
@@ -32,7 +34,8 @@ int main()
             ctd::PowerClass fn = ctd::refine_class(n, p - wt, true, cn, ctd::rare_q_of(p, 61));
             if ((p - 1) % 9 == 0)
                 fn = ctd::nine_class(n, p - wt, true, fn);
-            same = cn.M == c.M && cn.r == c.r && fn.M == f.M && fn.r == f.r;
+            const ctd::PowerClass cpn = ctd::doubling_class_by_pattern(n, p - wt, true);
+            same = same && cn.M == c.M && cn.r == c.r && fn.M == f.M && fn.r == f.r && cpn.M == c.M && cpn.r == c.r;
         }
         std::printf("%u %u %u %u %d %d %d\n", c.M, c.r, f.M, f.r, x, ctd::jacobi(wt, p), same);
     }

@@ -35,7 +35,7 @@ def classes(checker, cases):
 
 def both(got):
     """(M, r) of the base class and of the refined one, for each case"""
-    assert all(g[6] == 1 for g in got), "narrow Montgomery classes differ"
+    assert all(g[6] == 1 for g in got), "narrow Montgomery or pattern classes differ"
     return [((M, r), (M2, r2)) for M, r, M2, r2, _, _, _ in got]
 
 
@@ -51,7 +51,7 @@ def test_quadratic_screen_and_jacobi(checker):
     cases += [(p, w) for p in map(int, sympy.primerange(3, 200)) for w in range(1, p)]
     got = classes(checker, cases)
     screened = 0
-    assert all(g[6] == 1 for g in got), "narrow Montgomery classes differ"
+    assert all(g[6] == 1 for g in got), "narrow Montgomery or pattern classes differ"
     for (p, w), (M, _, M2, _, x, jac, _) in zip(cases, got):
         assert jac == sympy.jacobi_symbol(w, p), (p, w, jac)
         if x:
