@@ -81,10 +81,11 @@ PLAIN = {
 FAMILY_NAMES = {0: "MERSENNE", 1: "PROTH", 2: "RIESEL", 3: "SMARANDACHE", 4: "FIBONACCI", 5: "LUCAS",
                 6: "PROTH_FIXED_N", 7: "RIESEL_FIXED_N", 8: "TRIBONACCI"}
 # Roofline inputs per workload (what the dominant launch executes):
-#  * proth -- the classified doubling launch (screen_kernel, classify_kernel,
-#    refine_kernel, nine_kernel, regroup_kernel, class_walk_kernel): bound by
-#    integer issue slots.  Thread instructions and DRAM bytes per prime come
-#    from one ncu capture of the same six kernels on the 2^27-wide segment
+#  * proth -- the classified doubling launch (screen_kernel, classify_kernel
+#    once per divisibility pattern, refine_kernel, nine_kernel,
+#    regroup_kernel, class_walk_kernel): bound by integer issue slots.
+#    Thread instructions and DRAM bytes per prime come from one ncu capture
+#    of the same 13 launches on the 2^27-wide segment
 #    [2^32, 2^32 + 2^27) of this workload
 #    (6,047,768 primes; the capture's command is in the profile summary);
 #    the live launch time comes from CUDA events in this run.
@@ -96,11 +97,26 @@ FAMILY_NAMES = {0: "MERSENNE", 1: "PROTH", 2: "RIESEL", 3: "SMARANDACHE", 4: "FI
 #    shifts per block = 57/18 ALU operations per update, against the ALU
 #    compare rate measured now.
 PROTH_NCU = {"primes": 6047768,
-             "thread_inst": {"screen_kernel": 56524200 * 30.87, "classify_kernel": 1138696783 * 24.99,
-                             "refine_kernel": 288371018 * 24.44, "nine_kernel": 89598023 * 28.62,
-                             "regroup_kernel": 54846300 * 16.45, "class_walk_kernel": 1943662882 * 29.43},
-             "dram_bytes": (59.647488 + 12.317696 + 77.039616 + 13.650176 + 78.412288 + 1.800960 + 68.404480
-                            + 1.362176 + 72.984832 + 13.078528 + 53.844736 + 7.384576) * 1e6}
+             # warp instructions x active lanes per instruction, one entry per launch
+             "thread_inst": {
+                 "screen_kernel": 65171117 * 29.81,
+                 "classify_kernel_p0": 138376087 * 29.73,
+                 "classify_kernel_p1": 308210775 * 28.69,
+                 "classify_kernel_p2": 52839333 * 29.36,
+                 "classify_kernel_p3": 116957900 * 27.64,
+                 "classify_kernel_p4": 33193732 * 29.51,
+                 "classify_kernel_p5": 72399508 * 27.55,
+                 "classify_kernel_p6": 12661141 * 28.59,
+                 "classify_kernel_p7": 28061220 * 26.34,
+                 "refine_kernel": 287116277 * 24.54,
+                 "nine_kernel": 89272496 * 28.73,
+                 "regroup_kernel": 54846300 * 16.45,
+                 "class_walk_kernel": 1943762169 * 29.43},
+             # dram__bytes_read.sum + dram__bytes_write.sum of the same launches, MB
+             "dram_bytes": (62.117888 + 15.262720 + 55.312640 + 5.810688 + 63.984640 + 9.134592 + 31.630080
+                            + 1.137664 + 48.087296 + 3.818752 + 21.795840 + 0.343552 + 36.625408 + 1.915904
+                            + 8.099328 + 0.015872 + 15.641344 + 0.125952 + 79.052288 + 3.646464 + 68.420608
+                            + 1.735424 + 72.955648 + 12.934144 + 53.841920 + 7.536640) * 1e6}
 SMARANDACHE_MULS_PER_UPDATE = 3
 TRIBONACCI_ALU_OPS_PER_UPDATE = 57 / 18
 
@@ -450,12 +466,12 @@ def run_ours(args, world, rank, local):
         achieved = inst / launch_s
         roofline = {
             "bound": "int_issue",
-            "kernel": "screen_kernel<PROTH> + classify_kernel<PROTH> + refine_kernel<PROTH> + nine_kernel<PROTH> + "
-                      "regroup_kernel + class_walk_kernel<PROTH>",
+            "kernel": "screen_kernel<PROTH> + classify_kernel<PROTH, pattern> x 8 + refine_kernel<PROTH> + "
+                      "nine_kernel<PROTH> + regroup_kernel + class_walk_kernel<PROTH>",
             "achieved": achieved / 1e9, "peak": (peaks["int"] / 1e9) if peaks["int"] else None, "unit": "Ginst/s",
             "frac": (achieved / peaks["int"]) if peaks["int"] else None,
             "thread_instructions_per_update": inst / per_launch_updates, "launch_ms": launch_s * 1e3,
-            "achieved_source": "ncu thread instructions of the six kernels on a 2^27-segment of this workload, "
+            "achieved_source": "ncu thread instructions of the launch's 13 kernels on a 2^27-segment of this workload, "
                                "scaled by the primes per launch, over the CUDA-event launch time of this run",
             "peak_source": "measured now: libctd_probe add/xor chains (integer issue rate) on this GPU",
             "traffic": PROTH_NCU["dram_bytes"] / PROTH_NCU["primes"] * primes_launch,
