@@ -493,49 +493,51 @@ inline PowerClass doubling_class_by_pattern(const MT &m, uint64_t k, bool negate
     }
 }
 
-// ---- refinement by the character of a rarer prime q = 11 .. 61
+// ---- refinement by the character of a rarer prime q = 11 .. 127
 // A prime q divides p - 1 for one prime p in q - 1, and then its character
 // keeps one term in q (or none), so over the classes above the walk shrinks
-// by about prod (1 - 1/q) = 0.58 for q = 11 .. 61.  The refinement costs two
-// more full powers, for the primes that have such a q only: the kernels run
-// it as a separate pass over those primes (a quarter of them), so no warp
-// carries lanes that skip it.  It takes the smallest such q of each prime
-// (the one that shrinks the walk most): one power pair and one discrete
-// logarithm per prime, the same code for every lane whatever its q (taking
-// every q of the primes that have two or more ran the pass twice as long for
-// the extra 1/q of their walks).
-constexpr int POWRES_RARE_COUNT = 14;
-// the rare q, 6 bits each: 11, 13, 17, 19, 23, 29, 31, 37, 41, 43 | 47, 53, 59, 61
-constexpr uint64_t POWRES_RARE_LO = 11ull | 13ull << 6 | 17ull << 12 | 19ull << 18 | 23ull << 24 | 29ull << 30 |
-                                    31ull << 36 | 37ull << 42 | 41ull << 48 | 43ull << 54;
-constexpr uint64_t POWRES_RARE_HI = 47ull | 53ull << 6 | 59ull << 12 | 61ull << 18;
+// by about prod (1 - 1/q): 0.58 for q = 11 .. 61, 0.50 up to 127 (measured
+// over primes near 2^33: the walked fraction 0.063 -> 0.055 from 61 to 127).
+// The refinement costs two more full powers, for the primes that have such
+// a q only: the kernels run it as a separate pass over those primes (about
+// 30 % of them), so no warp carries lanes that skip it.  It takes the
+// smallest such q of each prime (the one that shrinks the walk most): one
+// power pair and one discrete logarithm per prime, the same code for every
+// lane whatever its q (taking every q of the primes that have two or more
+// ran the pass twice as long for the extra 1/q of their walks).
+constexpr int POWRES_RARE_COUNT = 27;
 CTD_HD uint32_t powres_rare_q(int i)
 {
-    return (uint32_t)((i < 10 ? POWRES_RARE_LO >> (6 * i) : POWRES_RARE_HI >> (6 * (i - 10))) & 63u);
+    constexpr uint8_t Q[POWRES_RARE_COUNT] = {11, 13, 17, 19, 23, 29, 31, 37, 41, 43, 47, 53, 59, 61, 67, 71,
+                                              73, 79, 83, 89, 97, 101, 103, 107, 109, 113, 127};
+    return Q[i];
 }
+// the rare q grouped into products below 2^32 (p - 1 is reduced once per
+// group in 64 bits, then by each q in 32 bits): the group of q_i
+constexpr int POWRES_RARE_GROUPS = 6;
+CTD_HD int powres_rare_group(int i) { return i < 6 ? 0 : i < 11 ? 1 : i < 16 ? 2 : i < 20 ? 3 : i < 24 ? 4 : 5; }
 // classes stay below 2^16: the walks' item code packs M and r in 16 bits
-// each (840 * 61 = 51240)
+// each (a merge past it is dropped; the class stays sound, only wider)
 constexpr uint32_t POWRES_MAX_M = 65535;
 
 // the smallest rare q <= qmax dividing p - 1; 0 when there is none
 CTD_HD uint32_t rare_q_of(uint64_t p, uint32_t qmax)
 {
     const uint64_t p1 = p - 1;
-    // three 64-bit reductions by products of the q, then 32-bit ones
-    const uint32_t r0 = (uint32_t)(p1 % (11ull * 13 * 17 * 19 * 23 * 29));
-    const uint32_t r1 = (uint32_t)(p1 % (31ull * 37 * 41 * 43 * 47));
-    const uint32_t r2 = (uint32_t)(p1 % (53ull * 59 * 61));
+    const uint32_t r[POWRES_RARE_GROUPS] = {
+        (uint32_t)(p1 % (11ull * 13 * 17 * 19 * 23 * 29)), (uint32_t)(p1 % (31ull * 37 * 41 * 43 * 47)),
+        (uint32_t)(p1 % (53ull * 59 * 61 * 67 * 71)),      (uint32_t)(p1 % (73ull * 79 * 83 * 89)),
+        (uint32_t)(p1 % (97ull * 101 * 103 * 107)),        (uint32_t)(p1 % (109ull * 113 * 127))};
     uint32_t found = 0;
 #pragma unroll
     for (int i = POWRES_RARE_COUNT - 1; i >= 0; --i) {
         const uint32_t q = powres_rare_q(i);
-        const uint32_t r = i < 6 ? r0 : i < 11 ? r1 : r2;
-        found = q <= qmax && r % q == 0 ? q : found;
+        found = q <= qmax && r[powres_rare_group(i)] % q == 0 ? q : found;
     }
     return found;
 }
 
-// j < q with z^j = y, for z of prime order q, 11 <= q <= 64 (baby steps
+// j < q with z^j = y, for z of prime order q, 11 <= q <= 127 (baby steps
 // z^0 .. z^7, giant steps by z^-8 = z^(q - 8)); q when there is none
 template <class MT>
 CTD_HD uint32_t small_log(const MT &m, uint64_t z, uint64_t y, uint32_t q)

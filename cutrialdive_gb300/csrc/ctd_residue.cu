@@ -1628,7 +1628,7 @@ __device__ __forceinline__ uint32_t class_bucket(uint32_t M)
 }
 
 // the largest rare prime of a job's refinement
-__device__ __forceinline__ uint32_t refine_qmax(const JobView &job) { return job.refine_q ? job.refine_q : 61u; }
+__device__ __forceinline__ uint32_t refine_qmax(const JobView &job) { return job.refine_q ? job.refine_q : 127u; }
 
 // whether a classified prime goes to the rare-prime refinement
 __device__ __forceinline__ bool wants_refine(const JobView &job, uint64_t p, uint32_t code)

@@ -115,8 +115,9 @@ typedef struct ctd_tuning {
     uint32_t variant;          /* step form, CTD_VARIANT_* (results never depend on it) */
     uint32_t classify_min;     /* Proth/Riesel/Mersenne: index ranges at least this long walk only the
                                   power-residue class of their zeros; 0 = 8192 */
-    uint32_t refine_q;         /* power-residue classes: the largest prime q (11..61) whose q-th power character
-                                  narrows them for the primes p with q | p - 1; 0 = 61, below 11 = none */
+    uint32_t refine_q;         /* power-residue classes: the largest prime q (11..127) whose q-th power character
+                                  narrows them for the primes p with q | p - 1; 0 = 127, below 11 = none
+                                  (the 9th-power character too) */
 } ctd_tuning;
 
 /* Step forms a tuning can select.  AUTO: the fastest measured form for the

@@ -2,7 +2,7 @@
 // (ctd_powres.cuh is __host__ __device__).  Reads "p wt" lines on stdin
 // (odd prime p, 0 < wt < p) and prints "M r M2 r2": every n with
 // 2^-n = wt (mod p) satisfies n = r (mod M), and n = r2 (mod M2) after the
-// refinement by the smallest rare prime q = 11 .. 61 dividing p - 1 and by
+// refinement by the smallest rare prime q = 11 .. 127 dividing p - 1 and by
 // the 9th-power character when 9 | p - 1; M = 0 (M2 = 0)
 // when no n does; then "x" (1 when the quadratic screen excludes p) and the
 // Jacobi symbol (wt/p); last 1 when the classes through the narrow
@@ -21,7 +21,7 @@ int main()
         m.init(p);
         // wt as -k with k = p - wt (the Proth form); the test covers every wt
         const ctd::PowerClass c = ctd::doubling_class(m, p - wt, true);
-        ctd::PowerClass f = ctd::refine_class(m, p - wt, true, c, ctd::rare_q_of(p, 61));
+        ctd::PowerClass f = ctd::refine_class(m, p - wt, true, c, ctd::rare_q_of(p, 127));
         if ((p - 1) % 9 == 0)
             f = ctd::nine_class(m, p - wt, true, f);
         const int x = ctd::quadratic_excluded(p, p - wt, true) ? 1 : 0;
@@ -31,7 +31,7 @@ int main()
             ctd::MontN n;
             n.init(p);
             const ctd::PowerClass cn = ctd::doubling_class(n, p - wt, true);
-            ctd::PowerClass fn = ctd::refine_class(n, p - wt, true, cn, ctd::rare_q_of(p, 61));
+            ctd::PowerClass fn = ctd::refine_class(n, p - wt, true, cn, ctd::rare_q_of(p, 127));
             if ((p - 1) % 9 == 0)
                 fn = ctd::nine_class(n, p - wt, true, fn);
             const ctd::PowerClass cpn = ctd::doubling_class_by_pattern(n, p - wt, true);
