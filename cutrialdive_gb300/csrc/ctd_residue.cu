@@ -443,8 +443,11 @@ __device__ __forceinline__ uint64_t plain_blocks(const uint32_t (&tlo)[BS], uint
 // that passed) and, on a match, the replay (all lanes together, so the warp
 // never splits).  That path keeps only the group's first state and steps
 // from it, so little stays live across the loop (the targets fill 32
-// registers) and its code exists once.
-constexpr int FILTER_GROUP = 8;
+// registers) and its code exists once.  Four blocks a group: over the
+// power-residue classes, where most giant steps are 64-bit Shoup products,
+// re-stepping into a group costs more than the extra votes (class walk on a
+// 2^27 Proth segment: 2.25 ms with groups of 8, 2.17 with 4, 2.24 with 2).
+constexpr int FILTER_GROUP = 4;
 template <typename Step, typename Replay>
 __device__ __forceinline__ uint64_t filtered_groups(const uint32_t (&tlo)[BS], uint64_t x, uint64_t ng, Step step,
                                                     Replay replay)
