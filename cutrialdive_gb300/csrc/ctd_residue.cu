@@ -1840,8 +1840,10 @@ __global__ void __launch_bounds__(256) nine_kernel(JobView job, const uint64_t *
 // the tile's classes in shared memory, one global atomic per class and tile
 // to reserve the tile's places in the class, then the scatter.  (One global
 // atomic per class and warp, as first written, left the kernel waiting on
-// atomics: long-scoreboard stalls of ~140 cycles per instruction.)
-constexpr int REGROUP_PER_THREAD = 16;
+// atomics: long-scoreboard stalls of ~140 cycles per instruction.)  Eight
+// primes a thread (16 took 103 registers and ran 0.14 ms on a 2^27 Proth
+// segment against 0.09 ms).
+constexpr int REGROUP_PER_THREAD = 8;
 __global__ void __launch_bounds__(256) regroup_kernel(const uint64_t *__restrict__ primes, uint64_t nprimes,
                                                       const uint32_t *__restrict__ codes, ClassCounters *__restrict__ cc,
                                                       ClassItem *__restrict__ items)
