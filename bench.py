@@ -100,23 +100,23 @@ PROTH_NCU = {"primes": 6047768,
              # warp instructions x active lanes per instruction, one entry per launch
              "thread_inst": {
                  "screen_kernel": 65171117 * 29.81,
-                 "classify_kernel_p0": 138376087 * 29.73,
-                 "classify_kernel_p1": 308210775 * 28.69,
-                 "classify_kernel_p2": 52839333 * 29.36,
-                 "classify_kernel_p3": 116957900 * 27.64,
-                 "classify_kernel_p4": 33193732 * 29.51,
-                 "classify_kernel_p5": 72399508 * 27.55,
-                 "classify_kernel_p6": 12661141 * 28.59,
-                 "classify_kernel_p7": 28061220 * 26.34,
-                 "refine_kernel": 287116277 * 24.54,
-                 "nine_kernel": 89272496 * 28.73,
-                 "regroup_kernel": 54846300 * 16.45,
-                 "class_walk_kernel": 1943762169 * 29.43},
+                 "classify_kernel_p0": 137905597 * 29.71,
+                 "classify_kernel_p1": 305578023 * 28.70,
+                 "classify_kernel_p2": 52691872 * 29.34,
+                 "classify_kernel_p3": 116636209 * 27.65,
+                 "classify_kernel_p4": 33097827 * 29.49,
+                 "classify_kernel_p5": 72198260 * 27.56,
+                 "classify_kernel_p6": 12630073 * 28.58,
+                 "classify_kernel_p7": 27994431 * 26.35,
+                 "refine_kernel": 368555377 * 22.68,
+                 "nine_kernel": 89261176 * 28.67,
+                 "regroup_kernel": 56827222 * 15.91,
+                 "class_walk_kernel": 1766376687 * 29.29},
              # dram__bytes_read.sum + dram__bytes_write.sum of the same launches, MB
-             "dram_bytes": (62.117888 + 15.262720 + 55.312640 + 5.810688 + 63.984640 + 9.134592 + 31.630080
-                            + 1.137664 + 48.087296 + 3.818752 + 21.795840 + 0.343552 + 36.625408 + 1.915904
-                            + 8.099328 + 0.015872 + 15.641344 + 0.125952 + 79.052288 + 3.646464 + 68.420608
-                            + 1.735424 + 72.955648 + 12.934144 + 53.841920 + 7.536640) * 1e6}
+             "dram_bytes": (62.131456 + 15.244032 + 55.497984 + 5.997056 + 64.804608 + 9.814016 + 31.731456 +
+                            1.238784 + 47.942912 + 3.658752 + 21.819648 + 0.367872 + 36.379648 + 1.655552 + 8.099584
+                            + 0.015616 + 15.653888 + 0.136192 + 80.845056 + 4.103168 + 68.398592 + 1.622784 +
+                            73.150464 + 11.985408 + 53.790464 + 7.205120) * 1e6}
 SMARANDACHE_MULS_PER_UPDATE = 3
 TRIBONACCI_ALU_OPS_PER_UPDATE = 57 / 18
 
