@@ -192,6 +192,30 @@ struct MontT {
         return w * mu() + (w * one - r) * ((uint64_t)0 - pinv);
     }
 
+    // the same quotient without r2: with W = w R mod p (the Montgomery form
+    // of w), w 2^64 = q p + W, so q = -W p^-1 = W pinv mod 2^64 (exact: q <
+    // 2^64).  W from doublings and additions of R mod p for w < 64, else
+    // from R^2 made here (six squarings of 2R)
+    CTD_HD uint64_t shoup_any(uint64_t w) const
+    {
+        uint64_t W = 0;
+        if (w < 64) {
+#pragma unroll
+            for (int b = 5; b >= 0; --b) {
+                W = dblmod(W, p);
+                if ((w >> b) & 1)
+                    W = addmod(W, one, p);
+            }
+        } else {
+            uint64_t x = dblmod(one, p);
+#pragma unroll
+            for (int i = 0; i < 6; ++i)
+                x = mul(x, x);
+            W = mul(w, x);
+        }
+        return W * pinv;
+    }
+
     // (2^e) in Montgomery form: left-to-right binary powering in which a set
     // bit costs a modular doubling instead of a multiplication.
     CTD_HD uint64_t pow2(uint64_t e) const

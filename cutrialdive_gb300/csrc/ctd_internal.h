@@ -130,6 +130,7 @@ struct ResidueScratch {
     uint32_t *codes = nullptr;
     ClassItem *items = nullptr;
     uint32_t *refine = nullptr;  // indices of the primes to refine
+    uint8_t *refine_q = nullptr; // and their rare q
     uint32_t *listed = nullptr;  // indices of the primes to classify: 8 lists of cap, by pattern
     uint32_t *nine = nullptr;    // indices of the primes for the 9th-power character
     uint64_t cap = 0;  // primes

@@ -206,13 +206,13 @@ CTD_HD bool quadratic_excluded(uint64_t p, uint64_t k, bool negate)
 // in one left-to-right loop over the bits of e: per bit a squaring of each,
 // and for a set bit a halving of A's Montgomery representative ((x R)/2 =
 // (x/2) R) and a Shoup multiplication of B by the plain k -- two
-// independent chains per iteration.  0 < e < p - 1, p < 2^63, m with r2.
+// independent chains per iteration.  0 < e < p - 1, p < 2^63 (m needs no r2).
 template <class MT>
 CTD_HD void power_pair(const MT &m, uint64_t k, bool negate, uint64_t e, uint64_t &A, uint64_t &B)
 {
     const uint64_t p = m.p;
     const uint64_t kr = k < p ? k : k % p;
-    const uint64_t ks = m.shoup(kr);
+    const uint64_t ks = m.shoup_any(kr);
     A = m.one;
     B = m.one;
     // A and B stay below 2p (the narrow product's lazy form; a halving of
@@ -232,8 +232,8 @@ CTD_HD void power_pair(const MT &m, uint64_t k, bool negate, uint64_t e, uint64_
 }
 
 // The class of the zeros of 2^-n = wt (mod p), wt = -k (negate) or k, for
-// an odd prime p < 2^63 and a plain k with k mod p != 0; m fully
-// initialised (r2 is needed for k's Shoup quotient).  The work is the same
+// an odd prime p < 2^63 and a plain k with k mod p != 0 (m needs no r2).
+// The work is the same
 // for every prime -- two full powers, fixed chains, loops of fixed length
 // -- so the lanes of a warp stay together.
 template <class MT>

@@ -622,7 +622,7 @@ __device__ __forceinline__ uint32_t doubling_class_code(const JobView &job, uint
     if (!k)
         return 0;  // p | k: k 2^n -+ 1 = -+1 (mod p), never zero
     MT m;
-    m.init(p);
+    m.init_lite(p);  // the power pairs need no R^2
     const PowerClass c = doubling_class(m, k, FAM == PROTH);
     return c.M ? (c.M << 16) | c.r : 0u;
 }
@@ -1651,20 +1651,19 @@ __device__ __forceinline__ uint32_t nine_code(const JobView &job, uint64_t p, ui
 {
     const uint64_t k = FAM == MERSENNE ? 1 : (job.param < p ? job.param : job.param % p);
     MT m;
-    m.init(p);
+    m.init_lite(p);  // the power pairs need no R^2
     const PowerClass c = nine_class(m, k, FAM == PROTH, PowerClass{code >> 16, code & 0xffffu});
     return c.M ? (c.M << 16) | c.r : 0u;
 }
 
 // the refined code of a classified prime (0: it divides no term)
 template <uint32_t FAM, class MT>
-__device__ __forceinline__ uint32_t refined_code(const JobView &job, uint64_t p, uint32_t code)
+__device__ __forceinline__ uint32_t refined_code(const JobView &job, uint64_t p, uint32_t code, uint32_t q)
 {
     const uint64_t k = FAM == MERSENNE ? 1 : (job.param < p ? job.param : job.param % p);
     MT m;
-    m.init(p);
-    const PowerClass c = refine_class(m, k, FAM == PROTH, PowerClass{code >> 16, code & 0xffffu},
-                                      rare_q_of(p, refine_qmax(job)));
+    m.init_lite(p);  // the power pairs need no R^2
+    const PowerClass c = refine_class(m, k, FAM == PROTH, PowerClass{code >> 16, code & 0xffffu}, q);
     return c.M ? (c.M << 16) | c.r : 0u;
 }
 
@@ -1733,7 +1732,7 @@ __device__ __forceinline__ uint32_t class_code_pat(const JobView &job, uint64_t 
     if (!k)
         return 0;
     MT m;
-    m.init(p);
+    m.init_lite(p);  // the power pairs need no R^2
     const PowerClass c = doubling_class_pat<PAT>(m, k, FAM == PROTH);
     return c.M ? (c.M << 16) | c.r : 0u;
 }
@@ -1741,8 +1740,8 @@ __device__ __forceinline__ uint32_t class_code_pat(const JobView &job, uint64_t 
 template <uint32_t FAM, int PAT, class MT>
 __device__ __forceinline__ void classify_range(const JobView &job, const uint64_t *__restrict__ primes, uint64_t n,
                                                uint32_t *__restrict__ codes, ClassCounters *__restrict__ cc,
-                                               uint32_t *__restrict__ refine, uint32_t *__restrict__ nine,
-                                               const uint32_t *__restrict__ listed)
+                                               uint32_t *__restrict__ refine, uint8_t *__restrict__ refine_q,
+                                               uint32_t *__restrict__ nine, const uint32_t *__restrict__ listed)
 {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
@@ -1750,8 +1749,12 @@ __device__ __forceinline__ void classify_range(const JobView &job, const uint64_
         const uint64_t p = primes[i];
         const uint32_t code = class_code_pat<FAM, PAT, MT>(job, p);
         codes[i] = code;
-        if (wants_refine(job, p, code))
-            refine[aggregated_increment(&cc->nrefine, 0)] = (uint32_t)i;
+        const uint32_t q = code && p < (1ull << 63) ? rare_q_of(p, refine_qmax(job)) : 0u;
+        if (q) {
+            const uint32_t at = aggregated_increment(&cc->nrefine, 0);
+            refine[at] = (uint32_t)i;
+            refine_q[at] = (uint8_t)q;
+        }
         else if (wants_nine(job, p, code))
             nine[aggregated_increment(&cc->nnine, 0)] = (uint32_t)i;
         else if (code)
@@ -1766,27 +1769,28 @@ __device__ __forceinline__ void classify_range(const JobView &job, const uint64_
 template <uint32_t FAM, int PAT>
 __global__ void __launch_bounds__(256, 4) classify_kernel(JobView job, const uint64_t *__restrict__ primes,
                                                        uint32_t *__restrict__ codes, ClassCounters *__restrict__ cc,
-                                                       uint32_t *__restrict__ refine, uint32_t *__restrict__ nine,
-                                                       const uint32_t *__restrict__ listed, uint64_t cap)
+                                                       uint32_t *__restrict__ refine, uint8_t *__restrict__ refine_q,
+                                                       uint32_t *__restrict__ nine, const uint32_t *__restrict__ listed,
+                                                       uint64_t cap)
 {
     const uint64_t n = cc->nlisted[PAT];
     if (cc->wide)
-        classify_range<FAM, PAT, Mont>(job, primes, n, codes, cc, refine, nine, listed + PAT * cap);
+        classify_range<FAM, PAT, Mont>(job, primes, n, codes, cc, refine, refine_q, nine, listed + PAT * cap);
     else
-        classify_range<FAM, PAT, MontN>(job, primes, n, codes, cc, refine, nine, listed + PAT * cap);
+        classify_range<FAM, PAT, MontN>(job, primes, n, codes, cc, refine, refine_q, nine, listed + PAT * cap);
 }
 
 template <uint32_t FAM, class MT>
 __device__ __forceinline__ void refine_range(const JobView &job, const uint64_t *__restrict__ primes,
                                              uint32_t *__restrict__ codes, ClassCounters *__restrict__ cc,
-                                             const uint32_t *__restrict__ refine, uint32_t *__restrict__ nine,
-                                             uint32_t n)
+                                             const uint32_t *__restrict__ refine, const uint8_t *__restrict__ refine_q,
+                                             uint32_t *__restrict__ nine, uint32_t n)
 {
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
         const uint32_t i = refine[t];
         const uint64_t p = primes[i];
-        const uint32_t code = refined_code<FAM, MT>(job, p, codes[i]);
+        const uint32_t code = refined_code<FAM, MT>(job, p, codes[i], refine_q[t]);
         codes[i] = code;
         if (wants_nine(job, p, code))
             nine[aggregated_increment(&cc->nnine, 0)] = i;
@@ -1800,12 +1804,13 @@ __device__ __forceinline__ void refine_range(const JobView &job, const uint64_t 
 template <uint32_t FAM>
 __global__ void __launch_bounds__(256) refine_kernel(JobView job, const uint64_t *__restrict__ primes,
                                                      uint32_t *__restrict__ codes, ClassCounters *__restrict__ cc,
-                                                     const uint32_t *__restrict__ refine, uint32_t *__restrict__ nine)
+                                                     const uint32_t *__restrict__ refine,
+                                                     const uint8_t *__restrict__ refine_q, uint32_t *__restrict__ nine)
 {
     if (cc->wide)
-        refine_range<FAM, Mont>(job, primes, codes, cc, refine, nine, cc->nrefine);
+        refine_range<FAM, Mont>(job, primes, codes, cc, refine, refine_q, nine, cc->nrefine);
     else
-        refine_range<FAM, MontN>(job, primes, codes, cc, refine, nine, cc->nrefine);
+        refine_range<FAM, MontN>(job, primes, codes, cc, refine, refine_q, nine, cc->nrefine);
 }
 
 template <uint32_t FAM, class MT>
@@ -2057,7 +2062,7 @@ __device__ __forceinline__ uint32_t class_code_rt(const JobView &v, uint64_t p)
     if (!k)
         return 0;
     MT m;
-    m.init(p);
+    m.init_lite(p);  // the power pairs need no R^2
     const PowerClass c = doubling_class(m, k, v.family == PROTH);
     return c.M ? (c.M << 16) | c.r : 0u;
 }
@@ -2066,7 +2071,7 @@ __device__ __forceinline__ uint32_t refined_code_rt(const JobView &v, uint64_t p
 {
     const uint64_t k = v.family == MERSENNE ? 1 : (v.param < p ? v.param : v.param % p);
     MT m;
-    m.init(p);
+    m.init_lite(p);  // the power pairs need no R^2
     const PowerClass c = refine_class(m, k, v.family == PROTH, PowerClass{code >> 16, code & 0xffffu},
                                       rare_q_of(p, refine_qmax(v)));
     return c.M ? (c.M << 16) | c.r : 0u;
@@ -2536,6 +2541,7 @@ void residue_scratch_destroy(ResidueScratch *rs)
     cudaFree(rs->codes);
     cudaFree(rs->items);
     cudaFree(rs->refine);
+    cudaFree(rs->refine_q);
     cudaFree(rs->listed);
     cudaFree(rs->nine);
     cudaFree(rs->counters);
@@ -2556,11 +2562,13 @@ static int ensure_class_scratch(ResidueScratch *rs, uint64_t nprimes, std::strin
     cudaFree(rs->codes);
     cudaFree(rs->items);
     cudaFree(rs->refine);
+    cudaFree(rs->refine_q);
     cudaFree(rs->listed);
     cudaFree(rs->nine);
     rs->codes = nullptr;
     rs->items = nullptr;
     rs->refine = nullptr;
+    rs->refine_q = nullptr;
     rs->listed = nullptr;
     rs->nine = nullptr;
     rs->cap = 0;
@@ -2569,6 +2577,8 @@ static int ensure_class_scratch(ResidueScratch *rs, uint64_t nprimes, std::strin
         e = cudaMalloc(&rs->items, nprimes * sizeof(ClassItem));
     if (e == cudaSuccess)
         e = cudaMalloc(&rs->refine, nprimes * sizeof(uint32_t));
+    if (e == cudaSuccess)
+        e = cudaMalloc(&rs->refine_q, nprimes);
     if (e == cudaSuccess)
         e = cudaMalloc(&rs->listed, 8 * nprimes * sizeof(uint32_t));
     if (e == cudaSuccess)
@@ -2614,7 +2624,7 @@ static int launch_classified(const JobView &v, const uint64_t *d_primes, uint64_
 #define CTD_CLASSIFY(PAT)                                                                                         \
     if (e == cudaSuccess) {                                                                                       \
         classify_kernel<FAM, PAT><<<cgrid, 256, 0, st>>>(v, d_primes, rs->codes, rs->counters, rs->refine,       \
-                                                         rs->nine, rs->listed, rs->cap);                          \
+                                                         rs->refine_q, rs->nine, rs->listed, rs->cap);            \
         e = cudaGetLastError();                                                                                   \
         if (e == cudaSuccess && PAT < 7)                                                                          \
             note_kernel_launch();                                                                                 \
@@ -2627,7 +2637,8 @@ static int launch_classified(const JobView &v, const uint64_t *d_primes, uint64_
         // the listed primes are about a quarter of n: a grid for that many
         const uint64_t rwant = (n / 4 + 255) / 256;
         const int rgrid = (int)(rwant < (uint64_t)rs->sm_count * 8 ? (rwant ? rwant : 1) : (uint64_t)rs->sm_count * 8);
-        refine_kernel<FAM><<<rgrid, 256, 0, st>>>(v, d_primes, rs->codes, rs->counters, rs->refine, rs->nine);
+        refine_kernel<FAM><<<rgrid, 256, 0, st>>>(v, d_primes, rs->codes, rs->counters, rs->refine, rs->refine_q,
+                                                  rs->nine);
         e = cudaGetLastError();
         if (e == cudaSuccess) {
             note_kernel_launch();

@@ -4,7 +4,8 @@
 // R mod p, R^2 mod p, 2^e mod p, k*2^e mod p (Montgomery form times plain k),
 // from(to(k)) for R = 2^64, floor(2^64 / p) and floor((k mod p) 2^64 / p);
 // then, for p < 2^40 (0 0 otherwise), 2^e mod p and (k mod p)(k/2^7 mod p)
-// R^-1 mod p through the narrow Montgomery product.
+// R^-1 mod p through the narrow Montgomery product; then the Shoup quotient
+// of k mod p without r2 (shoup_any), and of (k mod p) mod 64.
 #include <cinttypes>
 #include <cstdio>
 
@@ -25,9 +26,13 @@ int main()
             npow = n.from(n.pow2(e));
             nmul = n.mul(kk, (k >> 7) % p);
         }
+        ctd::Mont ml;
+        ml.init_lite(p);  // no r2
+        const uint64_t small = kk % 64 < p ? kk % 64 : 0;
         std::printf("%" PRIu64 " %" PRIu64 " %" PRIu64 " %" PRIu64 " %" PRIu64 " %" PRIu64 " %" PRIu64 " %" PRIu64
-                    " %" PRIu64 "\n",
-                    m.one, m.r2, m.from(U), m.mul(U, kk), m.from(m.to(k)), m.mu(), m.shoup(kk), npow, nmul);
+                    " %" PRIu64 " %" PRIu64 " %" PRIu64 " %" PRIu64 "\n",
+                    m.one, m.r2, m.from(U), m.mul(U, kk), m.from(m.to(k)), m.mu(), m.shoup(kk), npow, nmul,
+                    ml.shoup_any(kk), small, ml.shoup_any(small));
     }
     return 0;
 }

@@ -43,7 +43,7 @@ def test_montgomery_setup_and_pow2(checker):
     res = subprocess.run([checker], input=inp, capture_output=True, text=True, check=True).stdout.split("\n")
     R = 1 << 64
     for (p, e, k), line in zip(cs, res):
-        one, r2, pw, kpw, tok, mu, sh, npw, nmul = map(int, line.split())
+        one, r2, pw, kpw, tok, mu, sh, npw, nmul, sh_any, small, sh_small = map(int, line.split())
         assert one == R % p, (p, e)
         assert r2 == R * R % p, (p, e)
         assert pw == pow(2, e, p), (p, e)
@@ -51,6 +51,8 @@ def test_montgomery_setup_and_pow2(checker):
         assert tok == k % p, (p, k)
         assert mu == R // p, p
         assert sh == (k % p) * R // p, (p, k)
+        assert sh_any == sh, (p, k)  # the quotient without r2
+        assert sh_small == small * R // p, (p, small)
         if p < 1 << 40:  # the narrow Montgomery product
             assert npw == pow(2, e, p), (p, e)
             assert nmul == (k % p) * ((k >> 7) % p) * pow(R, -1, p) % p, (p, k)
