@@ -100,23 +100,23 @@ PROTH_NCU = {"primes": 6047768,
              # warp instructions x active lanes per instruction, one entry per launch
              "thread_inst": {
                  "screen_kernel": 65171117 * 29.81,
-                 "classify_kernel_p0": 137905597 * 29.71,
-                 "classify_kernel_p1": 305578023 * 28.70,
-                 "classify_kernel_p2": 52691872 * 29.34,
-                 "classify_kernel_p3": 116636209 * 27.65,
-                 "classify_kernel_p4": 33097827 * 29.49,
-                 "classify_kernel_p5": 72198260 * 27.56,
-                 "classify_kernel_p6": 12630073 * 28.58,
-                 "classify_kernel_p7": 27994431 * 26.35,
-                 "refine_kernel": 368555377 * 22.68,
-                 "nine_kernel": 89261176 * 28.67,
+                 "classify_kernel_p0": 132083823 * 29.59,
+                 "classify_kernel_p1": 296008858 * 28.57,
+                 "classify_kernel_p2": 50888238 * 29.23,
+                 "classify_kernel_p3": 113318332 * 27.48,
+                 "classify_kernel_p4": 32036834 * 29.39,
+                 "classify_kernel_p5": 70273674 * 27.39,
+                 "classify_kernel_p6": 12317771 * 28.46,
+                 "classify_kernel_p7": 27236171 * 26.17,
+                 "refine_kernel": 345691196 * 22.08,
+                 "nine_kernel": 85585714 * 28.52,
                  "regroup_kernel": 56827222 * 15.91,
-                 "class_walk_kernel": 1766376687 * 29.29},
+                 "class_walk_kernel": 1766405508 * 29.29},
              # dram__bytes_read.sum + dram__bytes_write.sum of the same launches, MB
-             "dram_bytes": (62.131456 + 15.244032 + 55.497984 + 5.997056 + 64.804608 + 9.814016 + 31.731456 +
-                            1.238784 + 47.942912 + 3.658752 + 21.819648 + 0.367872 + 36.379648 + 1.655552 + 8.099584
-                            + 0.015616 + 15.653888 + 0.136192 + 80.845056 + 4.103168 + 68.398592 + 1.622784 +
-                            73.150464 + 11.985408 + 53.790464 + 7.205120) * 1e6}
+             "dram_bytes": (62.139136 + 15.131648 + 55.799040 + 6.305024 + 64.647936 + 9.897216 + 31.821568 +
+                            1.323776 + 48.028160 + 3.731712 + 21.854976 + 0.397312 + 36.519936 + 1.793536 + 8.104448
+                            + 0.019200 + 15.659776 + 0.137728 + 82.969856 + 4.203776 + 68.397312 + 1.798656 +
+                            73.134592 + 11.983104 + 53.788672 + 7.094784) * 1e6}
 SMARANDACHE_MULS_PER_UPDATE = 3
 TRIBONACCI_ALU_OPS_PER_UPDATE = 57 / 18
 
