@@ -477,21 +477,6 @@ CTD_HD PowerClass doubling_class_pat(const MT &m, uint64_t k, bool negate)
     return c;
 }
 
-// doubling_class_pat for p's own pattern (host checks)
-template <class MT>
-inline PowerClass doubling_class_by_pattern(const MT &m, uint64_t k, bool negate)
-{
-    switch (powres_pattern(m.p)) {
-    case 0: return doubling_class_pat<0>(m, k, negate);
-    case 1: return doubling_class_pat<1>(m, k, negate);
-    case 2: return doubling_class_pat<2>(m, k, negate);
-    case 3: return doubling_class_pat<3>(m, k, negate);
-    case 4: return doubling_class_pat<4>(m, k, negate);
-    case 5: return doubling_class_pat<5>(m, k, negate);
-    case 6: return doubling_class_pat<6>(m, k, negate);
-    default: return doubling_class_pat<7>(m, k, negate);
-    }
-}
 
 // ---- refinement by the character of a rarer prime q = 11 .. 127
 // A prime q divides p - 1 for one prime p in q - 1, and then its character

@@ -611,22 +611,6 @@ __device__ __forceinline__ uint64_t doubling_target(const JobView &job, uint64_t
     return FAM == PROTH ? (k ? p - k : 0) : k;
 }
 
-// code of a prime's class: M << 16 | r, 0 when p divides no term; primes of
-// 2^63 and above keep the plain walk (M = 1)
-template <uint32_t FAM, class MT = Mont>
-__device__ __forceinline__ uint32_t doubling_class_code(const JobView &job, uint64_t p)
-{
-    if (p >= (1ull << 63))
-        return 1u << 16;
-    const uint64_t k = FAM == MERSENNE ? 1 : (job.param < p ? job.param : job.param % p);
-    if (!k)
-        return 0;  // p | k: k 2^n -+ 1 = -+1 (mod p), never zero
-    MT m;
-    m.init_lite(p);  // the power pairs need no R^2
-    const PowerClass c = doubling_class(m, k, FAM == PROTH);
-    return c.M ? (c.M << 16) | c.r : 0u;
-}
-
 // The doubling families for p >= 2^63 (beyond the classes' Shoup products):
 // the term-by-term walk of u = k 2^n with carry-safe doubling, out of line so
 // the class walks that call it for such primes keep their registers.
