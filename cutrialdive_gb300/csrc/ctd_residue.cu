@@ -2569,7 +2569,25 @@ static int ensure_class_scratch(ResidueScratch *rs, uint64_t nprimes, std::strin
         e = cudaMalloc(&rs->nine, nprimes * sizeof(uint32_t));
     if (e != cudaSuccess) {
         err = std::string("class scratch: ") + cudaGetErrorString(e);
-        return e == cudaErrorMemoryAllocation ? CTD_ERR_OUT_OF_MEMORY : CTD_ERR_CUDA;
+        // give back what was allocated, so that the caller's other path has
+        // the room, and clear the (non-sticky) allocation error
+        cudaFree(rs->codes);
+        cudaFree(rs->items);
+        cudaFree(rs->refine);
+        cudaFree(rs->refine_q);
+        cudaFree(rs->listed);
+        cudaFree(rs->nine);
+        rs->codes = nullptr;
+        rs->items = nullptr;
+        rs->refine = nullptr;
+        rs->refine_q = nullptr;
+        rs->listed = nullptr;
+        rs->nine = nullptr;
+        if (e == cudaErrorMemoryAllocation) {
+            (void)cudaGetLastError();
+            return CTD_ERR_OUT_OF_MEMORY;
+        }
+        return CTD_ERR_CUDA;
     }
     rs->cap = nprimes;
     return CTD_OK;
@@ -2663,10 +2681,21 @@ int launch_residues(const JobView &view, const uint64_t *d_primes, uint64_t npri
     // (the class passes index the primes with 32 bits)
     if (scratch && doubling && view.variant == CTD_VARIANT_AUTO && view.n1 - view.n0 >= cmin &&
         nprimes <= 0xffffffffull) {
-        switch (view.family) {
-        case PROTH: return launch_classified<PROTH>(view, d_primes, nprimes, stream, scratch, err);
-        case RIESEL: return launch_classified<RIESEL>(view, d_primes, nprimes, stream, scratch, err);
-        default: return launch_classified<MERSENNE>(view, d_primes, nprimes, stream, scratch, err);
+        // the class buffers (about 61 bytes a prime); without the device
+        // memory for them the walk over every term below gives the same
+        // factors
+        std::string serr;
+        const int src = ensure_class_scratch(scratch, nprimes, serr);
+        if (src == CTD_OK) {
+            switch (view.family) {
+            case PROTH: return launch_classified<PROTH>(view, d_primes, nprimes, stream, scratch, err);
+            case RIESEL: return launch_classified<RIESEL>(view, d_primes, nprimes, stream, scratch, err);
+            default: return launch_classified<MERSENNE>(view, d_primes, nprimes, stream, scratch, err);
+            }
+        }
+        if (src != CTD_ERR_OUT_OF_MEMORY) {
+            err = serr;
+            return src;
         }
     }
     // the work counter of the persistent grid (the context's scratch)
