@@ -100,23 +100,23 @@ PROTH_NCU = {"primes": 6047768,
              # warp instructions x active lanes per instruction, one entry per launch
              "thread_inst": {
                  "screen_kernel": 65171117 * 29.81,
-                 "classify_kernel_p0": 132083823 * 29.59,
-                 "classify_kernel_p1": 296008858 * 28.57,
-                 "classify_kernel_p2": 50888238 * 29.23,
-                 "classify_kernel_p3": 113318332 * 27.48,
-                 "classify_kernel_p4": 32036834 * 29.39,
-                 "classify_kernel_p5": 70273674 * 27.39,
-                 "classify_kernel_p6": 12317771 * 28.46,
-                 "classify_kernel_p7": 27236171 * 26.17,
-                 "refine_kernel": 345691196 * 22.08,
-                 "nine_kernel": 85585714 * 28.52,
-                 "regroup_kernel": 56827222 * 15.91,
-                 "class_walk_kernel": 1766405508 * 29.29},
+                 "classify_kernel_p0": 132079999 * 29.59,
+                 "classify_kernel_p1": 296012527 * 28.57,
+                 "classify_kernel_p2": 50881891 * 29.24,
+                 "classify_kernel_p3": 113313117 * 27.48,
+                 "classify_kernel_p4": 32032031 * 29.39,
+                 "classify_kernel_p5": 70274163 * 27.39,
+                 "classify_kernel_p6": 12315032 * 28.47,
+                 "classify_kernel_p7": 27235315 * 26.17,
+                 "refine_kernel": 289309073 * 26.81,
+                 "nine_kernel": 85534542 * 28.53,
+                 "regroup_kernel": 56933014 * 15.98,
+                 "class_walk_kernel": 1766393743 * 29.29},
              # dram__bytes_read.sum + dram__bytes_write.sum of the same launches, MB
-             "dram_bytes": (62.139136 + 15.131648 + 55.799040 + 6.305024 + 64.647936 + 9.897216 + 31.821568 +
-                            1.323776 + 48.028160 + 3.731712 + 21.854976 + 0.397312 + 36.519936 + 1.793536 + 8.104448
-                            + 0.019200 + 15.659776 + 0.137728 + 82.969856 + 4.203776 + 68.397312 + 1.798656 +
-                            73.134592 + 11.983104 + 53.788672 + 7.094784) * 1e6}
+             "dram_bytes": (62.006784 + 14.746624 + 55.477248 + 5.529600 + 64.505856 + 8.557056 + 31.603712 +
+                            1.104896 + 47.789312 + 3.366144 + 21.782528 + 0.321280 + 36.367616 + 1.626624 + 8.100096
+                            + 0.015616 + 15.639552 + 0.112640 + 83.481600 + 1.313792 + 68.398080 + 0.144128 +
+                            73.165568 + 8.725248 + 53.848832 + 5.083648) * 1e6}
 SMARANDACHE_MULS_PER_UPDATE = 3
 TRIBONACCI_ALU_OPS_PER_UPDATE = 57 / 18
 

@@ -1764,22 +1764,81 @@ __global__ void __launch_bounds__(256, 4) classify_kernel(JobView job, const uin
         classify_range<FAM, PAT, MontN>(job, primes, n, codes, cc, refine, refine_q, nine, listed + PAT * cap);
 }
 
+// Tiles of 256 x REFINE_PER_THREAD listed primes per CTA, sorted by their q
+// in shared memory before the powers: the logarithm's giant steps, z^(q-8)
+// and the inverse mod q run as long as the warp's largest q, so warps of
+// like q keep their lanes busy (in list order 22 of 32 lanes were active).
+constexpr int REFINE_PER_THREAD = 2;
 template <uint32_t FAM, class MT>
 __device__ __forceinline__ void refine_range(const JobView &job, const uint64_t *__restrict__ primes,
                                              uint32_t *__restrict__ codes, ClassCounters *__restrict__ cc,
                                              const uint32_t *__restrict__ refine, const uint8_t *__restrict__ refine_q,
                                              uint32_t *__restrict__ nine, uint32_t n)
 {
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
-        const uint32_t i = refine[t];
-        const uint64_t p = primes[i];
-        const uint32_t code = refined_code<FAM, MT>(job, p, codes[i], refine_q[t]);
-        codes[i] = code;
-        if (wants_nine(job, p, code))
-            nine[aggregated_increment(&cc->nnine, 0)] = i;
-        else if (code)
-            aggregated_increment(cc->count, class_bucket(code >> 16));
+    constexpr uint32_t TILE = 256 * REFINE_PER_THREAD;
+    __shared__ uint32_t start[128];  // per q: the tile's count, then its first place
+    __shared__ uint32_t sorted_i[TILE];
+    __shared__ uint8_t sorted_q[TILE];
+    const uint32_t tid = threadIdx.x;
+    for (uint64_t t0 = (uint64_t)blockIdx.x * TILE; t0 < n; t0 += (uint64_t)gridDim.x * TILE) {
+        if (tid < 128)
+            start[tid] = 0;
+        __syncthreads();
+        uint32_t idx[REFINE_PER_THREAD], q[REFINE_PER_THREAD], off[REFINE_PER_THREAD];
+        bool valid[REFINE_PER_THREAD];
+#pragma unroll
+        for (int j = 0; j < REFINE_PER_THREAD; ++j) {
+            const uint64_t t = t0 + (uint64_t)j * 256 + tid;
+            valid[j] = t < n;
+            if (valid[j]) {
+                idx[j] = refine[t];
+                q[j] = refine_q[t] & 127u;
+                off[j] = aggregated_increment(start, q[j]);
+            }
+        }
+        __syncthreads();
+        if (tid < 32) {  // exclusive scan of the 128 counts, four a lane
+            const uint32_t c0 = start[4 * tid], c1 = start[4 * tid + 1], c2 = start[4 * tid + 2],
+                           c3 = start[4 * tid + 3];
+            const uint32_t sum = c0 + c1 + c2 + c3;
+            uint32_t incl = sum;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
+                if ((int)tid >= d)
+                    incl += v;
+            }
+            const uint32_t base = incl - sum;
+            start[4 * tid] = base;
+            start[4 * tid + 1] = base + c0;
+            start[4 * tid + 2] = base + c0 + c1;
+            start[4 * tid + 3] = base + c0 + c1 + c2;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < REFINE_PER_THREAD; ++j)
+            if (valid[j]) {
+                const uint32_t at = start[q[j]] + off[j];
+                sorted_i[at] = idx[j];
+                sorted_q[at] = (uint8_t)q[j];
+            }
+        __syncthreads();
+        const uint32_t count = n - t0 < TILE ? (uint32_t)(n - t0) : TILE;
+#pragma unroll
+        for (int j = 0; j < REFINE_PER_THREAD; ++j) {
+            const uint32_t at = (uint32_t)j * 256 + tid;
+            if (at < count) {
+                const uint32_t i = sorted_i[at];
+                const uint64_t p = primes[i];
+                const uint32_t code = refined_code<FAM, MT>(job, p, codes[i], sorted_q[at]);
+                codes[i] = code;
+                if (wants_nine(job, p, code))
+                    nine[aggregated_increment(&cc->nnine, 0)] = i;
+                else if (code)
+                    aggregated_increment(cc->count, class_bucket(code >> 16));
+            }
+        }
+        __syncthreads();  // the next tile reuses the shared arrays
     }
 }
 
@@ -1842,9 +1901,11 @@ __global__ void __launch_bounds__(256) regroup_kernel(const uint64_t *__restrict
     __shared__ uint32_t tile_base[CLASS_BUCKETS];  // the tile's first place per class
     const uint32_t tid = threadIdx.x;
     if (tid < CLASS_BUCKETS) {
+        // a fixed trip count: the 48 loads go out together
         uint32_t run = 0;
-        for (uint32_t b = 0; b < tid; ++b)
-            run += cc->count[b];
+#pragma unroll
+        for (uint32_t b = 0; b < CLASS_BUCKETS; ++b)
+            run += b < tid ? cc->count[b] : 0u;
         base[tid] = run;
     }
     const uint64_t tile = (uint64_t)blockDim.x * REGROUP_PER_THREAD;
@@ -1881,6 +1942,7 @@ class_walk_kernel(JobView job, const ClassItem *__restrict__ items, ClassCounter
     __shared__ unsigned long long total_s;
     if (threadIdx.x == 0) {
         unsigned long long t = 0;
+#pragma unroll
         for (uint32_t b = 0; b < CLASS_BUCKETS; ++b)
             t += cc->count[b];
         total_s = t * job.tiles;
@@ -2637,7 +2699,8 @@ static int launch_classified(const JobView &v, const uint64_t *d_primes, uint64_
     if (e == cudaSuccess) {
         note_kernel_launch();
         // the listed primes are about a quarter of n: a grid for that many
-        const uint64_t rwant = (n / 4 + 255) / 256;
+        // (refine_kernel's tiles are 256 x REFINE_PER_THREAD of them)
+        const uint64_t rwant = (n / 4 + 256 * REFINE_PER_THREAD - 1) / (256 * REFINE_PER_THREAD);
         const int rgrid = (int)(rwant < (uint64_t)rs->sm_count * 8 ? (rwant ? rwant : 1) : (uint64_t)rs->sm_count * 8);
         refine_kernel<FAM><<<rgrid, 256, 0, st>>>(v, d_primes, rs->codes, rs->counters, rs->refine, rs->refine_q,
                                                   rs->nine);
