@@ -205,7 +205,10 @@ int ctd_sieve_device(ctd_ctx *ctx, uint64_t lo, uint64_t hi, uint64_t *d_out, ui
  * trial_div_by_odd_primes<Seq, 1, ...> implements (src/trial_factoring.cuh:156-228).
  * Asynchronous on `stream`; the launches use the context's scratch (work
  * counter, class buffers), so calls on one context must not overlap on
- * different streams. */
+ * different streams.  The class buffers of the Proth, Riesel and Mersenne
+ * launches (about 61 bytes per prime of the largest list, kept by the
+ * context) are allocated on first need; where the device cannot give them,
+ * the call walks every term instead, with the same results. */
 int ctd_residues_device(ctd_ctx *ctx, const ctd_job *job, const uint64_t *d_primes, uint64_t nprimes,
                         uint32_t *d_counts, uint64_t *d_factors, void *stream);
 
