@@ -614,7 +614,8 @@ int ctd_autotune(ctd_ctx *ctx, const ctd_job *job, double budget_s, ctd_tuning *
     ctd_tuning winner = base;
     const uint32_t fam = job->family;
     // power-residue classes (doubling families): always, or never; then the
-    // rare primes of their refinement: none, up to 31, all (up to 61)
+    // rare primes of their refinement: all (up to 127, the starting entry),
+    // none, up to 31
     if (!rc && (fam == CTD_PROTH || fam == CTD_RIESEL || fam == CTD_MERSENNE)) {
         for (uint32_t cm : {1u, 0xffffffffu}) {
             if (elapsed() >= budget_s)
