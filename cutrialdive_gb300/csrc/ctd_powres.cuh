@@ -41,7 +41,7 @@ struct PowerClass {
     uint32_t r;  // < M
 };
 
-// n = r (mod M) and n = j (mod q) for a prime q <= 64 not dividing M:
+// n = r (mod M) and n = j (mod q) for a prime q <= 127 not dividing M:
 // n = r + M t with t = (j - r) M^-1 (mod q), the inverse by Fermat
 // (M^(q-2)); 32-bit arithmetic
 CTD_HD void crt_merge_small(PowerClass &c, uint32_t j, uint32_t q)
@@ -549,7 +549,9 @@ CTD_HD uint32_t small_log(const MT &m, uint64_t z, uint64_t y, uint32_t q)
 // c (a class of doubling_class, M != 0) narrowed by the q-th power
 // character of q = rare_q_of(p, ...) (0: unchanged): with z = 2^-(p-1)/q
 // and y = wt^((p-1)/q), either z = 1 (no condition, or no zero at all when
-// y != 1) or n = log_z y (mod q).
+// y != 1) or n = log_z y (mod q).  M divides 420 here (where 8 | p - 1, 2
+// is a quadratic residue, so the 2-part of M is at most 4), so M q <= 420 *
+// 127 = 53340 stays within POWRES_MAX_M without a check.
 template <class MT>
 CTD_HD PowerClass refine_class(const MT &m, uint64_t k, bool negate, PowerClass c, uint32_t q)
 {

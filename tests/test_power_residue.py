@@ -97,6 +97,10 @@ def test_every_zero_lies_in_the_class(checker):
         order = int(sympy.n_order(2, p))
         member = pow(w, order, p) == 1  # w in <2^-1> = <2>
         (M0, r0), (M2, r2) = cls
+        # the classes of 2^3, 3, 5, 7 divide 420 (where 8 | p - 1, 2 is a
+        # quadratic residue: the 2-part is at most 4), so the refinement's
+        # M q stays below 420 * 127 < 2^16 with no check
+        assert M0 == 0 or 420 % M0 == 0, (p, w, M0)
         if M0 and M2:
             assert M2 % M0 == 0 and r2 % M0 == r0, (p, w, cls)  # a sub-class
             refined += M2 > M0
@@ -115,6 +119,32 @@ def test_every_zero_lies_in_the_class(checker):
                 assert pow(h, n, p) == w
                 assert n % M == r, (p, w, M, r, n)
     assert skipped > 0 and refined > 20, (skipped, refined)
+
+
+def test_largest_classes_fit_16_bits(checker):
+    """Primes p = 1 (mod 840 * 127), where the classes of 2^3, 3, 5, 7 reach
+    M = 420 and the refinement by q = 127 M = 53340: the walks' item code
+    keeps M and r in 16 bits each, and every zero still lies in the class."""
+    rnd = random.Random(17)
+    ps, k = [], 1
+    while len(ps) < 40:
+        if sympy.isprime(k * 840 * 127 + 1):
+            ps.append(k * 840 * 127 + 1)
+        k += 1
+    cases = [(p, w) for p in ps for w in (p - 3, rnd.randrange(1, p), rnd.randrange(1, p))]
+    got = both(classes(checker, cases))
+    assert max(M0 for (M0, _), _ in got) == 420
+    assert max(M2 for _, (M2, _) in got) == 420 * 127
+    for (p, w), cls in zip(cases, got):
+        h = pow(2, -1, p)
+        member = pow(w, int(sympy.n_order(2, p)), p) == 1
+        n = int(sympy.discrete_log(p, w, h)) if member else None
+        for M, r in cls:
+            assert 0 <= r < max(M, 1) and M <= 65535, (p, w, M, r)
+            if M:
+                assert n is None or n % M == r, (p, w, M, r, n)
+            else:
+                assert not member, (p, w)
 
 
 def test_small_primes_exhaustively(checker):
